@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Headline benchmark: SNICIT-form SDGC inference on one GB300.
+
+Workload (default "sdgc-4096x480"): N=4096 neurons, L=480 layers, a batch of
+B=60000 seeded binary inputs (per-row density 0.95*Beta(2,8), mean 0.19),
+32 nonzeros per weight row at 0.0625, bias -0.35, clamp 32.  One step = one
+full inference of the batch through the SNICIT path (plain layers up to the
+autotuned threshold, clustering, residue layers, recovery).  The plain
+per-layer path (SNIG mode) on the same batch is measured alongside.
+
+Metric: nominal SDGC edges/s = B * 32 * N * L / t (the reference paper's
+throughput definition), plus ms per inference.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU recurrence on the host cores.
+The reference ships no CPU implementation of the recurrence, so this arm runs
+the oracle's FP32 restatement of bf_inference (oracle/sdnn_oracle.c) on a
+bounded sample of the same workload with all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (N, L, B, bias, threshold default)
+    "sdgc-1024x120": (1024, 120, 60000, -0.30, 30),
+    "sdgc-4096x480": (4096, 480, 60000, -0.35, 30),
+    "sdgc-16384x1920": (16384, 1920, 60000, -0.40, 30),
+    "sdgc-65536x1920": (65536, 1920, 60000, -0.45, 30),
+}
+SEED = 20260101
+NNZ = 32
+METRIC = "edges/s & ms/inference, SNICIT vs plain on 1 GB300 (exact categories); p50/p99"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6777.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) < 9:
+                        continue
+                    try:
+                        sm.append(float(p[1]))
+                        mx = max(mx, float(p[2]))
+                    except ValueError:
+                        continue
+                    for n, v in zip(names, p[5:9]):
+                        if v.lower().startswith("active"):
+                            reasons.add(n)
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_layers_csr(sg, N, L):
+    return [sg.generate_layer_csr(N, SEED, l, NNZ, 0.0625) for l in range(L)]
+
+
+def cpu_port_rate(sg, N, L, bias, rows_budget_s=12.0, offset=0, layers=None):
+    """FP32 oracle port on a bounded sample; returns (edges/s, rows, seconds, threads)."""
+    from oracle import oracle as orc
+    if layers is None:
+        layers = make_layers_csr(sg, N, L)
+    threads = os.cpu_count() or 1
+    probe = max(threads, 32)
+    Y = sg.generate_inputs(N, SEED, offset, probe)
+    t0 = time.perf_counter()
+    orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
+    dt = time.perf_counter() - t0
+    rows = int(min(20000, max(probe, probe * rows_budget_s / max(dt, 1e-3))))
+    Y = sg.generate_inputs(N, SEED, offset, rows)
+    t0 = time.perf_counter()
+    orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
+    dt = time.perf_counter() - t0
+    return rows * NNZ * N * L / dt, rows, dt, threads, layers
+
+
+def run_reference(args):
+    import snicit_gb300 as sg
+    N, L, B, bias, _ = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    layers = make_layers_csr(sg, N, L)
+    rates = []
+    rows = secs = threads = 0
+    for step in range(args.warmup + args.steps):
+        budget = 4.0 if step < args.warmup else 12.0
+        r, rows, secs, threads, _ = cpu_port_rate(sg, N, L, bias, budget, offset=step * 997,
+                                                  layers=layers)
+        if step >= args.warmup:
+            rates.append(r)
+    value = statistics.median(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "edges/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": B * NNZ * N * L / value * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "neurons": N, "layers": L, "batch": B,
+                   "nnz_per_row": NNZ, "bias": bias, "mode": "plain recurrence (bf_inference)",
+                   "note": "ms_per_step extrapolated from the bounded sample"},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} rows of the {B}-row batch per step, all {L} layers, "
+                                   f"{secs:.1f} s; the reference has no CPU recurrence "
+                                   "(src/SDGC/utils/header.h:7-10), so this is the oracle's FP32 "
+                                   "restatement of bf_inference"},
+        "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import snicit_gb300 as sg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    N, L, B, bias, t_default = WORKLOADS[args.workload]
+    threshold = args.threshold if args.threshold is not None else t_default
+    # each rank runs its own batch (weak scaling over independent samples)
+    Y0 = sg.generate_inputs(N, SEED, rank * B, B)
+    edges = float(B) * NNZ * N * L
+
+    eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=B, bias=bias,
+                    num_centroids=args.centroids, device=local)
+    eng.generate_weights(SEED, NNZ, 0.0625)
+    eng.finalize()
+    tune = None
+    if not args.no_autotune:
+        rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
+        os.makedirs(os.path.dirname(rec), exist_ok=True)
+        if os.path.exists(rec):
+            os.remove(rec)
+        tune = eng.autotune(Y0[: args.tune_rows], rec)
+
+    d_in = torch.from_numpy(Y0).to(f"cuda:{local}")
+    d_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    st = eng.stats()
+    flags_ref = d_flags.cpu().numpy().copy()
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pre_ms, per_step = [], []
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            step()
+            s1.record(stream)
+            per_step.append((s0, s1))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    if dist:
+        dist.barrier()
+    st = eng.stats()  # stage events of the last step
+    step_ms = [a.elapsed_time(b) for a, b in per_step]
+    flags = d_flags.cpu().numpy()
+    assert np.array_equal(flags, flags_ref), "category set changed between steps"
+    t = torch.tensor([elapsed_ms], dtype=torch.float64)
+    if dist:
+        t = t.cuda()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world * edges * args.steps / (max_ms / 1e3)
+    ms_per_step = max_ms / args.steps
+
+    # plain per-layer path on the same batch (the comparison point)
+    plain = sg.Engine(N, L, mode="SNIG", batch=B, bias=bias, device=local,
+                      tile_rows=tune["tile_rows"] if tune else 0,
+                      threads=tune["threads"] if tune else 0)
+    plain.generate_weights(SEED, NNZ, 0.0625)
+    plain_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
+    for _ in range(2):
+        plain.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    psteps = max(1, min(args.steps, 3))
+    p0.record(stream)
+    for _ in range(psteps):
+        plain.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1) / psteps
+    pst = plain.stats()
+    plain_exact = bool(np.array_equal(plain_flags.cpu().numpy(), flags))
+
+    # roofline of the dominant kernel: the plain layer kernel of the pre-threshold stage
+    nnz_layer = st["weight_nnz"] / L
+    T = st["threshold"]
+    pre_bytes = 8.0 * N * st["pre_row_layers"] + 4.0 * st["pre_row_layers"] + 8.0 * nnz_layer * T
+    pre_s = st["stage_ms"][0] / 1e3
+    peak, peak_kind = peaks()
+    achieved = pre_bytes / pre_s / 1e9 if pre_s > 0 else 0.0
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"layer_kernel_{args.workload}.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    launches_pre = max(1, T)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "sdnn::layer_kernel (plain epilogue)", "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": pre_bytes / launches_pre,
+                "avg_launch_ms": st["stage_ms"][0] / launches_pre,
+                "frac_of_8tbs": achieved / 8000.0}
+
+    # end to end through the public host API: pinned host inputs in, survivor ids out
+    pinned = torch.from_numpy(Y0).pin_memory()
+    host = pinned.numpy()
+    eng.infer(host, want_flags=False, want_ids=True)
+    e2e_t = []
+    count = 0
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        _, ids = eng.infer(host, want_flags=False, want_ids=True)
+        e2e_t.append(time.perf_counter() - t0)
+        count = len(ids)
+    assert count == int(flags.sum())
+    e2e_s = statistics.median(e2e_t)
+    e2e = {"value": world * edges / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": B * N * 4,
+           "d2h_bytes_per_step": 4 + 4 * count, "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r, rows, secs, threads, _ = cpu_port_rate(sg, N, L, bias, args.cpu_seconds)
+        cpu = {"value": r, "unit": "edges/s", "cores": threads, "kind": "port",
+               "sample": f"first {rows} rows of the batch, all {L} layers, {secs:.1f} s "
+                         "(FP32 restatement of bf_inference)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "neurons": N, "layers": L, "batch": B,
+                       "nnz_per_row": NNZ, "bias": bias, "mode": "SNICIT",
+                       "threshold": st["threshold"], "centroids_kept": st["centroids"],
+                       "centroid_candidates": eng.cfg.num_centroids,
+                       "tile_rows": st["tile_rows"], "threads": st["threads"],
+                       "l2": "inputs (B*N*4 bytes) larger than L2",
+                       "parallelism": f"replicas x{world} (independent batches)"},
+            "p50_ms": statistics.median(step_ms),
+            "p99_ms": sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))],
+            "survivors": int(flags.sum()),
+            "stage_ms": st["stage_ms"],
+            "plain": {"ms_per_inference": plain_ms, "edges_per_s": edges / (plain_ms / 1e3),
+                      "category_set_equal": plain_exact, "row_layers": pst["row_layers"]},
+            "speedup_vs_plain": plain_ms / ms_per_step,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": st["launches"] * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    plain.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sdgc-4096x480", choices=sorted(WORKLOADS))
+    ap.add_argument("--threshold", type=int, default=None)
+    ap.add_argument("--centroids", type=int, default=50)
+    ap.add_argument("--tune-rows", type=int, default=4096)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * snicit_gb300.h -- C ABI of the GB300 sparse-DNN inference engine.
+ *
+ * The engine computes the SDGC recurrence
+ *     Y[l+1] = min(max(Y[l] * W[l] + b, 0), clamp)
+ * over L sparse layers of N neurons, in one of the reference's four modes
+ * (BF, SNIG, XY, SNICIT), and returns the category set: the ids of the
+ * samples whose final row has any nonzero entry.
+ *
+ * Reference interfaces this ABI replaces (paths are inside IDEA-CUHK/SNICIT):
+ *   - main/SDGC.cu:13-110             CLI flags -m -n -l -t -b, bias map, dispatch
+ *   - src/SDGC/base.hpp:69-141        Base ctor + weight loading (packed CSR)
+ *   - src/SDGC/utility.hpp:85-191     TSV -> CSR / dense input loaders
+ *   - src/SDGC/BF/BF.hpp:102-124      BF::infer
+ *   - src/SDGC/SNIG/SNIG.hpp:100-130  SNIG::infer
+ *   - src/SDGC/XY/XY.hpp              XY::infer
+ *   - src/SDGC/SNICIT/SNICIT.hpp:87-203  SNICIT::infer
+ *   - src/SDGC/utility.hpp:194-212    identify (category per sample)
+ * The reference exposes header-only C++ classes whose constructor takes
+ * (weight_path, bias, N, L[, threshold]) and whose infer() takes
+ * (input_path, golden_path, num_inputs[, batch]); errors there end the
+ * process (Safe_Call -> exit) or throw.  Here every call returns an int
+ * status (sdnn_status), never exits and takes no locks.  One engine owns one
+ * CUDA stream and all of its buffers and must be driven by one host thread at
+ * a time; separate engines may run concurrently.
+ *
+ * All pointers are plain host pointers unless the name says "device".
+ */
+#ifndef SNICIT_GB300_H
+#define SNICIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDNN_ABI_VERSION 1
+
+/* Status codes returned by every entry point. */
+typedef enum sdnn_status {
+  SDNN_OK = 0,
+  SDNN_ERR_INVALID = 1,     /* bad argument or unsupported shape            */
+  SDNN_ERR_CUDA = 2,        /* a CUDA runtime call failed                   */
+  SDNN_ERR_OOM = 3,         /* device or host allocation failed             */
+  SDNN_ERR_IO = 4,          /* a file could not be opened or written        */
+  SDNN_ERR_FORMAT = 5,      /* malformed TSV / binary content               */
+  SDNN_ERR_STATE = 6,       /* call out of order (e.g. infer before weights) */
+  SDNN_ERR_TIMEOUT = 7,     /* a device-side bounded wait gave up           */
+  SDNN_ERR_UNSUPPORTED = 8, /* feature not available in this build          */
+  SDNN_ERR_BUSY = 9         /* serving: no slot / memory free for a request */
+} sdnn_status;
+
+/* Execution modes: the reference's -m values (main/SDGC.cu:15-20). */
+typedef enum sdnn_mode {
+  SDNN_MODE_BF = 0,     /* plain per-layer kernel, one launch per layer     */
+  SDNN_MODE_SNIG = 1,   /* plain kernel, whole layer loop as one CUDA graph */
+  SDNN_MODE_XY = 2,     /* plain kernel in a graph, pre/post timing split   */
+  SDNN_MODE_SNICIT = 3  /* threshold clustering + residue update + recovery */
+} sdnn_mode;
+
+typedef struct sdnn_config {
+  int32_t num_neurons;   /* -n  N (multiple of 32)                               */
+  int32_t num_layers;    /* -l  L                                                */
+  int32_t mode;          /* -m  sdnn_mode                                        */
+  int32_t threshold;     /* -t  SNICIT threshold layer (layers < t are plain)    */
+  int64_t batch;         /* -b  maximum rows per inference call                   */
+  float bias;            /* scalar bias (main/SDGC.cu:49-54 bias_map)             */
+  float clamp;           /* upper clamp of the activation (32 in SDGC)            */
+  int32_t num_centroids; /* SNICIT centroid candidates (reference: 32)            */
+  int32_t autotune;      /* 1: let sdnn_autotune choose threshold/centroids/tile  */
+  uint64_t seed;         /* seed of the centroid candidate pick                   */
+  int32_t device;        /* CUDA device ordinal                                   */
+  int32_t tile_rows;     /* rows per CTA in the layer kernel (0 = automatic)      */
+  int32_t threads;       /* threads per CTA in the layer kernel (0 = automatic)   */
+  int32_t reserved[5];
+} sdnn_config;
+
+/* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
+typedef struct sdnn_stats {
+  float stage_ms[4];     /* pre-threshold, clustering, post-threshold, recovery */
+  float total_ms;        /* device time of the whole inference                 */
+  int64_t rows_in;       /* rows submitted                                     */
+  int64_t rows_out;      /* size of the category set                           */
+  int64_t row_layers;    /* sum over layers of rows processed (plain rows +    */
+                         /* centroid + non-empty residue rows)                 */
+  int32_t centroids;     /* SNICIT: centroids kept after pruning               */
+  int32_t residue_rows;  /* SNICIT: non-empty residue rows at the threshold    */
+  int32_t launches;      /* kernel launches of the last inference              */
+  int32_t threshold;     /* threshold layer used                               */
+  int32_t tile_rows;     /* tile rows used by the layer kernel                 */
+  int32_t threads;       /* threads per CTA used by the layer kernel           */
+  int32_t reserved0;
+  int64_t pre_row_layers;   /* rows processed by the plain layers (sum)        */
+  int64_t post_row_layers;  /* centroid + residue rows of the post layers      */
+  int64_t weight_nnz;       /* nonzeros of all L layers                        */
+  int32_t reserved[4];
+} sdnn_stats;
+
+typedef struct sdnn_engine sdnn_engine;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+
+/* Fills *cfg with the reference defaults: N=1024, L=120, mode SNICIT, t=30,
+ * batch 60000, bias from the reference bias map, clamp 32, 32 candidates. */
+int sdnn_config_default(sdnn_config* cfg);
+
+/* Reference bias per neuron count (main/SDGC.cu:49-54); 0 for unknown N. */
+float sdnn_reference_bias(int32_t num_neurons);
+
+/* Replaces the engine constructors (BF.hpp BF::BF, SNICIT.hpp SNICIT::SNICIT). */
+int sdnn_create(const sdnn_config* cfg, sdnn_engine** out);
+int sdnn_destroy(sdnn_engine* e);
+
+/* Human-readable text of the last error on this engine ("" if none). */
+const char* sdnn_last_error(const sdnn_engine* e);
+const char* sdnn_status_string(int status);
+int sdnn_abi_version(void);
+
+/* ---- weights ------------------------------------------------------------ */
+
+/* Reads dir/n{N}-l{l}.tsv for l = 1..L: one "row<TAB>col<TAB>value" line per
+ * nonzero, 1-based, row = input neuron, col = output neuron; duplicate
+ * entries are summed (Eigen setFromTriplets semantics).
+ * Replaces read_weight / tsv_string_to_CSR_packed_array
+ * (src/SDGC/utility.hpp:85-157) and Base::_load_weight (src/SDGC/base.hpp:89-141). */
+int sdnn_load_weights_tsv(sdnn_engine* e, const char* dir);
+
+/* One layer from 0-based COO triplets (row = input, col = output). */
+int sdnn_set_layer_coo(sdnn_engine* e, int32_t layer, const int32_t* rows,
+                       const int32_t* cols, const float* vals, int64_t nnz);
+
+/* Per-neuron bias of one layer (the beyond nets, src/beyond/general.hpp:36-72).
+ * Without this call every layer uses cfg->bias. */
+int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias);
+
+/* Synthetic SDGC-shaped weights: every input row gets nnz_per_row distinct
+ * output columns drawn uniformly without replacement, all with `value`.
+ * Column draws are a counter-based SplitMix64 stream keyed by
+ * (seed, layer, row). */
+int sdnn_generate_weights(sdnn_engine* e, uint64_t seed, int32_t nnz_per_row, float value);
+
+/* Packs the host weights into the device layout (bank-scheduled slots) and
+ * uploads them.  Called implicitly by the first inference. */
+int sdnn_finalize_weights(sdnn_engine* e);
+
+/* ---- inference ---------------------------------------------------------- */
+
+/* Host-buffer inference: Y0 is rows x N row-major FP32 on the host.  Copies
+ * in, runs the configured mode, copies the category set out.
+ *   flags      (optional) rows ints, 1 if the sample survives (identify)
+ *   ids        (optional) up to rows ints, sorted 0-based survivor ids
+ *   count      (optional) number of survivors
+ * Replaces BF::infer / SNIG::infer / XY::infer / SNICIT::infer minus the
+ * golden-file check. */
+int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows,
+                    int32_t* flags, int32_t* ids, int64_t* count);
+
+/* Device-resident inference on the engine's stream (cudaStream_t passed as
+ * void*; NULL = the engine's own).  d_Y0 rows x N FP32 device pointer,
+ * d_flags rows int32 device pointer.  Does not synchronize. */
+int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
+                      int32_t* d_flags, void* stream);
+
+/* Inputs read from a reference-format TSV ("sample<TAB>feature<TAB>value",
+ * 1-based), rows [row_offset, row_offset + rows) into a host buffer
+ * (src/SDGC/utility.hpp:160-191,268-293). */
+int sdnn_read_inputs_tsv(const char* path, int32_t num_neurons, int64_t row_offset,
+                         int64_t rows, float* out);
+
+/* Final activations of the last inference, rows x N, neuron order of the
+ * reference (SNICIT rows are recovered: centroid + residue). */
+int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows);
+
+/* Statistics of the last inference. */
+int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
+
+/* Chooses threshold, centroid count and tile shape by timing the candidates
+ * on the given sample rows (host buffer) and appends one JSON line per tried
+ * setting to record_path (if not NULL).  Applies the fastest setting. */
+int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows, const char* record_path);
+
+/* ---- synthetic data and reference file formats --------------------------- */
+
+/* Seeded binary inputs: row r has density rho_r = 0.95 * (2nd smallest of 9
+ * uniform draws) (mean 0.19) and entries 1 with probability rho_r.  Rows
+ * [row_offset, row_offset + rows) of the stream, written to out (rows x N). */
+int sdnn_generate_inputs(int32_t num_neurons, uint64_t seed, int64_t row_offset,
+                         int64_t rows, float* out);
+
+/* One synthetic layer as COO (rows/cols/vals each num_neurons * nnz_per_row). */
+int sdnn_generate_layer_coo(int32_t num_neurons, uint64_t seed, int32_t layer,
+                            int32_t nnz_per_row, float value, int32_t* rows,
+                            int32_t* cols, float* vals);
+
+/* Writers for the reference formats: weights dir/n{N}-l{l}.tsv, inputs
+ * sparse-images-{N}.tsv, categories one 1-based id per line. */
+int sdnn_write_weights_tsv(sdnn_engine* e, const char* dir);
+int sdnn_write_inputs_tsv(const char* path, const float* Y0, int64_t rows, int32_t num_neurons);
+int sdnn_write_categories_tsv(const char* path, const int32_t* ids, int64_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SNICIT_GB300_H */

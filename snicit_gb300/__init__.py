@@ -1,0 +1,10 @@
+"""GB300-native SNICIT sparse-DNN inference engine (sm_103a CUDA behind a C ABI).
+
+The compute path is the CUDA library built in-tree (libsnicit_gb300.so);
+this package only binds it.  See include/snicit_gb300.h for the ABI.
+"""
+from ._lib import MODES, SdnnError, load  # noqa: F401
+from .engine import (Engine, coo_to_csr, generate_inputs, generate_layer_coo,  # noqa: F401
+                     generate_layer_csr, read_inputs_tsv, write_categories_tsv,
+                     write_inputs_tsv)
+from .sdgc import BF, SNICIT, SNIG, XY  # noqa: F401

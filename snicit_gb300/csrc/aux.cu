@@ -1,0 +1,376 @@
+// Row-list utilities, category identification, the SNICIT threshold stage
+// (candidate pick, pruning, nearest-centroid residue conversion) and recovery.
+#include <climits>
+#include "sdnn_internal.h"
+
+namespace sdnn {
+
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static int grid_for(long work, int per_block, int cap = 4096) {
+  long g = (work + per_block - 1) / per_block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+// ---------------------------------------------------------------- row lists
+
+__global__ void iota_kernel(int32_t* list, int32_t* count, int32_t n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) list[i] = i;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
+}
+void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s) {
+  iota_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, count, n);
+}
+
+__global__ void mark_rows_kernel(const int32_t* list, const int32_t* count, int32_t* flags,
+                                 int32_t value) {
+  const int n = *count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    flags[list[i]] = value;
+}
+void launch_mark_rows(const int32_t* list, const int32_t* count, int32_t* flags, int32_t value,
+                      cudaStream_t s) {
+  mark_rows_kernel<<<264, 256, 0, s>>>(list, count, flags, value);
+}
+
+// identify (src/SDGC/utility.hpp:194-212): category = 1 if the row has an
+// activation > 0.  (The reference sums the row with thrust::reduce and an int
+// initial value; see the oracle for that variant.)  One warp per listed row.
+__global__ void identify_kernel(const float* __restrict__ y, const int32_t* list,
+                                const int32_t* count, int32_t N, int32_t* flags) {
+  const int n = *count;
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = wid; i < n; i += nw) {
+    const int r = list[i];
+    const float* row = y + (size_t)r * N;
+    bool any = false;
+    for (int j = lane; j < N && !any; j += 32) any = row[j] > 0.f;
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0) flags[r] = any ? 1 : 0;
+  }
+}
+void launch_identify(const float* y, const int32_t* list, const int32_t* count, int32_t N,
+                     int32_t* flags, cudaStream_t s) {
+  identify_kernel<<<528, 256, 0, s>>>(y, list, count, N, flags);
+}
+
+// Ordered compaction: ids = sorted indices i with flags[i] != 0.  One CTA.
+__global__ void __launch_bounds__(1024) flags_to_ids_kernel(const int32_t* flags, int32_t n,
+                                                            int32_t* ids, int32_t* count) {
+  __shared__ int wsum[32];
+  __shared__ int s_total;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int base = 0;
+  for (int start = 0; start < n; start += 4096) {
+    int f[4];
+    int local = 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = start + tid * 4 + u;
+      f[u] = (i < n && flags[i] != 0) ? 1 : 0;
+      local += f[u];
+    }
+    // inclusive warp scan of local
+    int inc = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += v;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      int w = wsum[lane];
+      int winc = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, winc, o);
+        if (lane >= o) winc += v;
+      }
+      wsum[lane] = winc - w;
+      if (lane == 31) s_total = winc;
+    }
+    __syncthreads();
+    int pos = base + wsum[warp] + inc - local;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (f[u]) ids[pos++] = start + tid * 4 + u;
+    base += s_total;
+    __syncthreads();
+  }
+  if (tid == 0) *count = base;
+}
+void launch_flags_to_ids(const int32_t* flags, int32_t n, int32_t* ids, int32_t* count,
+                         cudaStream_t s) {
+  flags_to_ids_kernel<<<1, 1024, 0, s>>>(flags, n, ids, count);
+}
+
+// ------------------------------------------------------- SNICIT threshold stage
+//
+// Reference: reduction + centroid_sel (src/SDGC/SNICIT/kernel.hpp:138-194),
+// host y* compaction (src/SDGC/SNICIT/SNICIT.hpp:457-462), coarse_cluster
+// (kernel.hpp:8-69) and the host ne_record -> rowsY pass (SNICIT.hpp:505-509).
+// Differences, by design: candidates are a seeded pick of K live rows (the
+// reference takes the first 32 rows of the batch); the 16 downsampling bins
+// are disjoint N/16-neuron ranges for every N; the centroid pick and the
+// residue list are built on the device.
+
+constexpr int kHistBins = 4096;
+constexpr int kCandCap = 2048;
+
+__global__ void __launch_bounds__(1024) cand_select_kernel(ClusterArgs a) {
+  __shared__ int hist[kHistBins];
+  __shared__ unsigned long long skey[kCandCap];
+  __shared__ int srow[kCandCap];
+  __shared__ int s_cut, s_n;
+  const int tid = threadIdx.x;
+  const int n = *a.live_count;
+  const int K = a.K;
+  for (int i = tid; i < kHistBins; i += blockDim.x) hist[i] = 0;
+  if (tid == 0) s_n = 0;
+  __syncthreads();
+  for (int i = tid; i < n; i += blockDim.x) {
+    const uint64_t key = mix64(a.seed ^ mix64((uint64_t)a.live[i]));
+    atomicAdd(&hist[key >> 52], 1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int cum = 0, cut = kHistBins - 1;
+    for (int b = 0; b < kHistBins; ++b) {
+      cum += hist[b];
+      if (cum >= K) {
+        cut = b;
+        break;
+      }
+    }
+    s_cut = cut;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += blockDim.x) {
+    const int r = a.live[i];
+    const uint64_t key = mix64(a.seed ^ mix64((uint64_t)r));
+    if ((int)(key >> 52) <= s_cut) {
+      const int pos = atomicAdd(&s_n, 1);
+      if (pos < kCandCap) {
+        skey[pos] = key;
+        srow[pos] = r;
+      }
+    }
+  }
+  __syncthreads();
+  const int m = min(s_n, kCandCap);
+  int M = 1;
+  while (M < m) M <<= 1;
+  for (int i = m + tid; i < M; i += blockDim.x) {
+    skey[i] = ~0ull;
+    srow[i] = INT_MAX;
+  }
+  __syncthreads();
+  // bitonic sort on (key, row)
+  for (int k = 2; k <= M; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < M; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const bool up = (i & k) == 0;
+          const unsigned long long ki = skey[i], kj = skey[ixj];
+          const int ri = srow[i], rj = srow[ixj];
+          const bool gt = (ki > kj) || (ki == kj && ri > rj);
+          if (gt == up) {
+            skey[i] = kj;
+            skey[ixj] = ki;
+            srow[i] = rj;
+            srow[ixj] = ri;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const int nc = min(K, m);
+  for (int i = tid; i < nc; i += blockDim.x) a.cand[i] = srow[i];
+  if (tid == 0) *a.ncand = nc;
+}
+
+// 16 disjoint bin sums per candidate; one warp per bin, fixed reduction order.
+__global__ void cand_bins_kernel(ClusterArgs a) {
+  const int k = blockIdx.x;
+  if (k >= *a.ncand) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float* row = a.y + (size_t)a.cand[k] * a.N;
+  const int w = a.N / 16;
+  for (int b = warp; b < 16; b += blockDim.x >> 5) {
+    float s = 0.f;
+    for (int j = b * w + lane; j < (b + 1) * w; j += 32) s += row[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) a.bins[k * 16 + b] = s;
+  }
+}
+
+// Greedy pruning (paper Alg. 1; centroid_sel, src/SDGC/SNICIT/kernel.hpp:156-194):
+// candidate k is dropped when an earlier kept candidate has every one of the 16
+// bins within 0.03 (the reference drops when fewer than 16*0.03 bins differ by
+// more than 0.03, i.e. when none does).
+__global__ void __launch_bounds__(256) prune_kernel(ClusterArgs a) {
+  __shared__ int keep[256];
+  __shared__ float sb[256 * 16];
+  const int tid = threadIdx.x;
+  const int nc = min(*a.ncand, 256);
+  for (int i = tid; i < nc * 16; i += blockDim.x) sb[i] = a.bins[i];
+  if (tid < nc) keep[tid] = 1;
+  __syncthreads();
+  for (int k = 1; k < nc; ++k) {
+    bool similar = false;
+    if (tid < k && keep[tid]) {
+      similar = true;
+      for (int b = 0; b < 16; ++b)
+        if (fabsf(sb[k * 16 + b] - sb[tid * 16 + b]) > 0.03f) {
+          similar = false;
+          break;
+        }
+    }
+    const int any = __syncthreads_or(similar);
+    if (tid == 0 && any) keep[k] = 0;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    int ci = 0;
+    for (int k = 0; k < nc; ++k) {
+      if (!keep[k]) continue;
+      const int r = a.cand[k];
+      a.clist[ci] = r;
+      a.cslot[r] = ci;
+      a.is_centroid[r] = 1;
+      ++ci;
+    }
+    *a.ccount = ci;
+  }
+}
+
+// Nearest centroid by L0 distance (count of differing entries), ties to the
+// lowest centroid index, residue written in place: y[r] <- y[r] - c.  Rows at
+// distance 0 get no residue and are left out of the residue list.
+__global__ void assign_kernel(ClusterArgs a) {
+  const int n = *a.live_count;
+  const int nc = *a.ccount;
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int N = a.N;
+  for (int i = wid; i < n; i += nw) {
+    const int r = a.live[i];
+    if (a.is_centroid[r]) continue;
+    float* yr = a.y + (size_t)r * N;
+    int best = INT_MAX, bk = 0;
+    for (int k = 0; k < nc; ++k) {
+      const float* yc = a.y + (size_t)a.clist[k] * N;
+      int dl = 0, dt = 0;
+      for (int j0 = 0; j0 < N; j0 += 1024) {
+        const int j1 = min(N, j0 + 1024);
+        for (int j = j0 + lane; j < j1; j += 32) dl += (yr[j] != yc[j]) ? 1 : 0;
+        dt = __reduce_add_sync(0xffffffffu, dl);
+        if (dt >= best) break;
+      }
+      if (dt < best) {
+        best = dt;
+        bk = k;
+        if (best == 0) break;
+      }
+    }
+    if (lane == 0) a.cslot[r] = bk;
+    if (best > 0) {
+      const float* yc = a.y + (size_t)a.clist[bk] * N;
+      for (int j = lane; j < N; j += 32) yr[j] = yr[j] - yc[j];
+      if (lane == 0) {
+        const int pos = atomicAdd(a.rcount, 1);
+        a.rlist[pos] = r;
+      }
+    }
+  }
+}
+
+void launch_cluster(const ClusterArgs& a, int num_sms, cudaStream_t s) {
+  cand_select_kernel<<<1, 1024, 0, s>>>(a);
+  cand_bins_kernel<<<a.K, 512, 0, s>>>(a);
+  prune_kernel<<<1, 256, 0, s>>>(a);
+  assign_kernel<<<num_sms * 4, 256, 0, s>>>(a);
+}
+
+// ------------------------------------------------------------------ recovery
+
+// recover (src/SDGC/SNICIT/kernel.hpp:197-218): flags[r] = any((delta + c) > 0).
+__global__ void recover_kernel(const float* __restrict__ y, const int32_t* live,
+                               const int32_t* live_count, const int32_t* cslot,
+                               const int32_t* clist, const int32_t* is_centroid,
+                               const int32_t* res_flag, int32_t N, int32_t* flags) {
+  const int n = *live_count;
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = wid; i < n; i += nw) {
+    const int r = live[i];
+    const float* yr = y + (size_t)r * N;
+    bool any = false;
+    if (is_centroid[r]) {
+      for (int j = lane; j < N && !any; j += 32) any = yr[j] > 0.f;
+    } else {
+      const float* yc = y + (size_t)clist[cslot[r]] * N;
+      if (res_flag[r]) {
+        for (int j = lane; j < N && !any; j += 32) any = (yr[j] + yc[j]) > 0.f;
+      } else {
+        for (int j = lane; j < N && !any; j += 32) any = yc[j] > 0.f;
+      }
+    }
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0) flags[r] = any ? 1 : 0;
+  }
+}
+void launch_recover(const float* y, const int32_t* live, const int32_t* live_count,
+                    const int32_t* cslot, const int32_t* clist, const int32_t* is_centroid,
+                    const int32_t* res_flag, int32_t N, int32_t* flags, cudaStream_t s) {
+  recover_kernel<<<528, 256, 0, s>>>(y, live, live_count, cslot, clist, is_centroid, res_flag, N,
+                                     flags);
+}
+
+// Final activations per row: state 0 -> zeros (dead), 1 -> copy of the final
+// buffer (plain modes), 2 -> SNICIT recovery (centroid, or centroid + residue).
+__global__ void materialize_kernel(const float* __restrict__ y, const int32_t* state,
+                                   const int32_t* cslot, const int32_t* clist,
+                                   const int32_t* is_centroid, const int32_t* res_flag,
+                                   int32_t N, int32_t rows, float* out) {
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    float* o = out + (size_t)r * N;
+    const int st = state[r];
+    const float* yr = y + (size_t)r * N;
+    if (st == 0) {
+      for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = 0.f;
+    } else if (st == 1 || is_centroid[r]) {
+      for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = yr[j];
+    } else {
+      const float* yc = y + (size_t)clist[cslot[r]] * N;
+      if (res_flag[r]) {
+        for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = yr[j] + yc[j];
+      } else {
+        for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = yc[j];
+      }
+    }
+  }
+}
+void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
+                        const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
+                        int32_t N, float* out, int32_t rows, cudaStream_t s) {
+  materialize_kernel<<<grid_for(rows, 1, 8192), 256, 0, s>>>(y, state, cslot, clist, is_centroid,
+                                                             res_flag, N, rows, out);
+}
+
+}  // namespace sdnn

@@ -1,0 +1,963 @@
+// The inference engine behind the C ABI (include/snicit_gb300.h).
+//
+// One engine = one CUDA stream + device-resident weights + row buffers.
+// The layer loop is device-driven: every kernel reads its row count from
+// device memory and compacts its survivors on the device, so no host
+// synchronisation happens between layers (the reference synchronises and
+// compacts on the host every layer, src/SDGC/SNICIT/SNICIT.hpp:548-630,
+// src/SDGC/BF/BF.hpp:198-207).  In SNIG, XY and SNICIT modes the whole
+// sequence is captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sdnn_internal.h"
+#include "snicit_gb300.h"
+#include "wpack.h"
+
+namespace sdnn {
+int read_weight_tsv(const std::string& path, int32_t N, HostLayer& out, std::string& err);
+int write_weight_tsv(const std::string& path, const HostLayer& h, int32_t N);
+void gen_row_cols(uint64_t seed, int32_t layer, int32_t row, int32_t N, int32_t nnz, int32_t* cols);
+}  // namespace sdnn
+
+using namespace sdnn;
+
+namespace {
+
+struct DevLayer {
+  uint2* idx = nullptr;
+  float4* val = nullptr;
+  int32_t* grp = nullptr;
+  float* bias = nullptr;
+  bool constw = true;
+  float wconst = 0.f;
+  int64_t nnz = 0;
+  int64_t slots = 0;
+  int32_t max_depth = 0;
+};
+
+struct GenSpec {
+  bool on = false;
+  uint64_t seed = 0;
+  int32_t nnz = 32;
+  float value = 0.0625f;
+};
+
+}  // namespace
+
+struct sdnn_engine {
+  sdnn_config cfg{};
+  std::string err;
+  int N = 0, L = 0, dev = 0, num_sms = 0;
+  cudaStream_t stream = nullptr;
+
+  // host-side weights
+  std::vector<HostLayer> hw;
+  std::vector<std::vector<float>> hbias;
+  GenSpec gen;
+  bool weights_dirty = true;
+
+  // kernel configuration
+  int Q = 0, nq = 1, G = 0;
+  LayerKernelKey key{};
+  int threads = 512, grid = 0, min_split = 1;
+  size_t smem = 0;
+
+  // device weights
+  std::vector<DevLayer> dl;
+  int64_t total_nnz = 0;
+
+  // device buffers
+  int64_t cap = 0;
+  int Kmax = 0;
+  float* d_y[2] = {nullptr, nullptr};
+  int32_t* d_list[2] = {nullptr, nullptr};
+  int32_t* d_rlist[2] = {nullptr, nullptr};
+  int32_t* d_counts = nullptr;   // [L + 2]
+  int32_t* d_rcounts = nullptr;  // [L + 2]
+  uint32_t* d_tmask = nullptr;
+  int32_t* d_ticket = nullptr;
+  int32_t* d_clist = nullptr;
+  int32_t* d_ccount = nullptr;
+  int32_t* d_cand = nullptr;
+  int32_t* d_ncand = nullptr;
+  float* d_bins = nullptr;
+  int32_t* d_cslot = nullptr;
+  int32_t* d_iscent = nullptr;
+  int32_t* d_resflag = nullptr;
+  int32_t* d_flags = nullptr;
+  int32_t* d_state = nullptr;
+  float* d_pre = nullptr;
+  int32_t* d_err = nullptr;
+  int32_t* d_ids = nullptr;
+  int32_t* d_idcount = nullptr;
+  float* d_in = nullptr;
+
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+
+  // graph cache
+  cudaGraphExec_t gexec = nullptr;
+  int64_t g_rows = -1;
+  const float* g_in = nullptr;
+  int32_t* g_flags = nullptr;
+  int g_T = -1, g_K = -1, g_mode = -1, g_tile = -1, g_threads = -1;
+
+  // last run
+  int64_t last_rows = 0;
+  int last_T = 0;
+  int launches = 0;
+  bool have_run = false;
+  int pending_stats = 0;
+  sdnn_stats stats{};
+};
+
+namespace {
+
+int fail(sdnn_engine* e, int code, const std::string& msg) {
+  if (e) e->err = msg;
+  return code;
+}
+int cuda_fail(sdnn_engine* e, cudaError_t rc, const char* what) {
+  return fail(e, SDNN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(rc));
+}
+#define CK(call)                                             \
+  do {                                                       \
+    cudaError_t _rc = (call);                                \
+    if (_rc != cudaSuccess) return cuda_fail(e, _rc, #call); \
+  } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+void free_weights(sdnn_engine* e) {
+  for (auto& d : e->dl) {
+    dfree(d.idx);
+    dfree(d.val);
+    dfree(d.grp);
+    dfree(d.bias);
+  }
+  e->dl.clear();
+}
+
+void free_buffers(sdnn_engine* e) {
+  dfree(e->d_y[0]);
+  dfree(e->d_y[1]);
+  dfree(e->d_list[0]);
+  dfree(e->d_list[1]);
+  dfree(e->d_rlist[0]);
+  dfree(e->d_rlist[1]);
+  dfree(e->d_counts);
+  dfree(e->d_rcounts);
+  dfree(e->d_tmask);
+  dfree(e->d_ticket);
+  dfree(e->d_clist);
+  dfree(e->d_ccount);
+  dfree(e->d_cand);
+  dfree(e->d_ncand);
+  dfree(e->d_bins);
+  dfree(e->d_cslot);
+  dfree(e->d_iscent);
+  dfree(e->d_resflag);
+  dfree(e->d_flags);
+  dfree(e->d_state);
+  dfree(e->d_pre);
+  dfree(e->d_err);
+  dfree(e->d_ids);
+  dfree(e->d_idcount);
+  dfree(e->d_in);
+  e->cap = 0;
+}
+
+void drop_graph(sdnn_engine* e) {
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  e->gexec = nullptr;
+  e->g_rows = -1;
+}
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+// Chooses chunking, kernel instance, tile rows, threads and grid.
+int choose_kernel(sdnn_engine* e) {
+  const int N = e->N;
+  e->Q = N > 32768 ? 16384 : N;
+  e->nq = N / e->Q;
+  e->G = N / 32;
+  const int req_T = e->cfg.tile_rows;
+  int threads = e->cfg.threads > 0 ? e->cfg.threads : 512;
+  if (threads != 256 && threads != 512) threads = 512;
+  std::vector<LayerKernelKey> cands;
+  if (e->nq == 1) {
+    int rsw = e->Q == 1024 ? 1056 : e->Q == 4096 ? 4128 : e->Q == 16384 ? 16416 : 0;
+    std::vector<int> Ts;
+    if (rsw == 1056) Ts = {32, 24, 16, 8};
+    else if (rsw == 4128) Ts = {8, 12, 6, 4, 2};
+    else if (rsw == 16416) Ts = {3, 2, 1};
+    else Ts = {8, 4, 2, 1};
+    for (int T : Ts) cands.push_back({T, rsw, 1, true});
+    if (rsw != 0)
+      for (int T : {8, 4, 2, 1}) cands.push_back({T, 0, 1, true});
+  } else {
+    if (e->Q == 16384)
+      for (int T : {3, 2, 1}) cands.push_back({T, 16416, 16, true});
+    cands.push_back({1, 0, 16, true});
+  }
+  for (const auto& k : cands) {
+    if (req_T > 0 && k.T != req_T) continue;
+    const size_t smem = (size_t)k.T * (size_t)(e->Q + 32) * 4;
+    if (smem > kMaxSmem) continue;
+    if (!layer_instance_exists(k)) continue;
+    LayerKernelKey kc = k, kg = k;
+    kc.constw = true;
+    kg.constw = false;
+    const int b1 = layer_blocks_per_sm(kc, threads, smem);
+    const int b2 = layer_blocks_per_sm(kg, threads, smem);
+    if (b1 <= 0 || b2 <= 0) continue;
+    e->key = k;
+    e->smem = smem;
+    e->threads = threads;
+    e->grid = e->num_sms * std::min(b1, b2);
+    const int nwarps = threads / 32;
+    e->min_split = k.kg > 1 ? (e->G + nwarps * k.kg - 1) / (nwarps * k.kg) : 1;
+    return SDNN_OK;
+  }
+  return fail(e, SDNN_ERR_UNSUPPORTED,
+              "no layer kernel instance fits N=" + std::to_string(N) +
+                  (req_T > 0 ? " with tile_rows=" + std::to_string(req_T) : std::string()));
+}
+
+int ensure_buffers(sdnn_engine* e, int64_t rows) {
+  if (e->cap >= rows && e->cap > 0) return SDNN_OK;
+  free_buffers(e);
+  drop_graph(e);
+  const int64_t cap = std::max<int64_t>(rows, e->cfg.batch);
+  const size_t N = (size_t)e->N;
+  const int K = std::max(1, e->cfg.num_centroids);
+  e->Kmax = K;
+  auto A = [&](auto** p, size_t bytes) -> cudaError_t {
+    return cudaMalloc((void**)p, std::max<size_t>(bytes, 16));
+  };
+  cudaError_t rc = cudaSuccess;
+  auto T = [&](cudaError_t r) {
+    if (rc == cudaSuccess) rc = r;
+  };
+  T(A(&e->d_y[0], (size_t)cap * N * 4));
+  T(A(&e->d_y[1], (size_t)cap * N * 4));
+  T(A(&e->d_in, (size_t)cap * N * 4));
+  for (int i = 0; i < 2; ++i) {
+    T(A(&e->d_list[i], (size_t)cap * 4));
+    T(A(&e->d_rlist[i], (size_t)cap * 4));
+  }
+  T(A(&e->d_counts, (size_t)(e->L + 4) * 4));
+  T(A(&e->d_rcounts, (size_t)(e->L + 4) * 4));
+  T(A(&e->d_tmask, (size_t)(cap + 1) * 4));
+  T(A(&e->d_ticket, (size_t)(cap + 1) * 4));
+  T(A(&e->d_clist, (size_t)K * 4));
+  T(A(&e->d_ccount, 16));
+  T(A(&e->d_cand, (size_t)K * 4));
+  T(A(&e->d_ncand, 16));
+  T(A(&e->d_bins, (size_t)K * 16 * 4));
+  T(A(&e->d_cslot, (size_t)cap * 4));
+  T(A(&e->d_iscent, (size_t)cap * 4));
+  T(A(&e->d_resflag, (size_t)cap * 4));
+  T(A(&e->d_flags, (size_t)cap * 4));
+  T(A(&e->d_state, (size_t)cap * 4));
+  T(A(&e->d_pre, (size_t)K * N * 4));
+  T(A(&e->d_err, 16));
+  T(A(&e->d_ids, (size_t)cap * 4));
+  T(A(&e->d_idcount, 16));
+  if (rc != cudaSuccess) {
+    free_buffers(e);
+    cudaGetLastError();
+    return fail(e, SDNN_ERR_OOM, std::string("device allocation failed: ") + cudaGetErrorString(rc));
+  }
+  e->cap = cap;
+  CK(cudaMemsetAsync(e->d_tmask, 0, (size_t)(cap + 1) * 4, e->stream));
+  CK(cudaMemsetAsync(e->d_ticket, 0, (size_t)(cap + 1) * 4, e->stream));
+  CK(cudaMemsetAsync(e->d_err, 0, 16, e->stream));
+  return SDNN_OK;
+}
+
+// Builds one layer (generated or given), packs it and uploads it.
+int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
+  HostLayer tmp;
+  const HostLayer* h = nullptr;
+  if (e->gen.on) {
+    const int N = e->N, k = e->gen.nnz;
+    tmp.row_off.resize(N + 1);
+    tmp.cols.resize((size_t)N * k);
+    tmp.vals.assign((size_t)N * k, e->gen.value);
+    for (int j = 0; j < N; ++j) {
+      tmp.row_off[j] = j * k;
+      int32_t* c = tmp.cols.data() + (size_t)j * k;
+      gen_row_cols(e->gen.seed, l, j, N, k, c);
+      std::sort(c, c + k);
+    }
+    tmp.row_off[N] = N * k;
+    tmp.present = true;
+    h = &tmp;
+  } else {
+    if (!e->hw[l].present) {
+      err = "layer " + std::to_string(l) + " has no weights";
+      return SDNN_ERR_STATE;
+    }
+    h = &e->hw[l];
+  }
+  PackedLayer p;
+  pack_layer(*h, e->N, e->Q, p);
+  DevLayer d;
+  d.constw = p.constw;
+  d.wconst = p.wconst;
+  d.nnz = p.nnz;
+  d.slots = p.slots;
+  d.max_depth = p.max_depth;
+  cudaError_t rc = cudaSuccess;
+  auto T = [&](cudaError_t r) {
+    if (rc == cudaSuccess) rc = r;
+  };
+  T(cudaMalloc((void**)&d.idx, std::max<size_t>(p.idx.size() * 2, 16)));
+  T(cudaMalloc((void**)&d.grp, p.grp_blk.size() * 4));
+  if (!p.constw) T(cudaMalloc((void**)&d.val, std::max<size_t>(p.val.size() * 4, 16)));
+  if (l < (int)e->hbias.size() && !e->hbias[l].empty())
+    T(cudaMalloc((void**)&d.bias, (size_t)e->N * 4));
+  if (rc == cudaSuccess && !p.idx.empty())
+    T(cudaMemcpy(d.idx, p.idx.data(), p.idx.size() * 2, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess) T(cudaMemcpy(d.grp, p.grp_blk.data(), p.grp_blk.size() * 4, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess && d.val && !p.val.empty())
+    T(cudaMemcpy(d.val, p.val.data(), p.val.size() * 4, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess && d.bias)
+    T(cudaMemcpy(d.bias, e->hbias[l].data(), (size_t)e->N * 4, cudaMemcpyHostToDevice));
+  e->dl[l] = d;
+  if (rc != cudaSuccess) {
+    err = std::string("weight upload failed: ") + cudaGetErrorString(rc);
+    return rc == cudaErrorMemoryAllocation ? SDNN_ERR_OOM : SDNN_ERR_CUDA;
+  }
+  return SDNN_OK;
+}
+
+int finalize_weights(sdnn_engine* e) {
+  if (!e->weights_dirty) return SDNN_OK;
+  if (!e->gen.on) {
+    if ((int)e->hw.size() != e->L) return fail(e, SDNN_ERR_STATE, "weights not loaded");
+    for (int l = 0; l < e->L; ++l)
+      if (!e->hw[l].present)
+        return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
+  }
+  drop_graph(e);
+  free_weights(e);
+  e->dl.assign(e->L, DevLayer{});
+  int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  nthreads = std::min(nthreads, e->L);
+  std::atomic<int> next{0};
+  std::atomic<int> status{SDNN_OK};
+  std::vector<std::string> errs(nthreads);
+  auto worker = [&](int id) {
+    cudaSetDevice(e->dev);
+    for (;;) {
+      const int l = next.fetch_add(1);
+      if (l >= e->L || status.load() != SDNN_OK) break;
+      const int rc = pack_upload_layer(e, l, errs[id]);
+      if (rc != SDNN_OK) {
+        int expected = SDNN_OK;
+        status.compare_exchange_strong(expected, rc);
+        break;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nthreads; ++i) pool.emplace_back(worker, i);
+  for (auto& t : pool) t.join();
+  if (status.load() != SDNN_OK) {
+    std::string msg;
+    for (auto& s : errs)
+      if (!s.empty()) msg = s;
+    free_weights(e);
+    return fail(e, status.load(), msg);
+  }
+  e->total_nnz = 0;
+  for (auto& d : e->dl) e->total_nnz += d.nnz;
+  e->weights_dirty = false;
+  return SDNN_OK;
+}
+
+int layer_launch(sdnn_engine* e, int l, int epi, const float* in, float* out, const int32_t* lin,
+                 const int32_t* cin, int32_t* lout, int32_t* cout) {
+  const DevLayer& d = e->dl[l];
+  LayerArgs a{};
+  a.w.idx = d.idx;
+  a.w.val = d.val;
+  a.w.grp_blk = d.grp;
+  a.w.bias_vec = d.bias;
+  a.w.bias = e->cfg.bias;
+  a.w.wconst = d.wconst;
+  a.y_in = in;
+  a.y_out = out;
+  a.list_in = lin;
+  a.count_in = cin;
+  a.list_out = lout;
+  a.count_out = cout;
+  a.tile_mask = e->d_tmask;
+  a.tile_ticket = e->d_ticket;
+  a.pre_out = e->d_pre;
+  a.pre_in = e->d_pre;
+  a.cslot = e->d_cslot;
+  a.err = e->d_err;
+  a.N = e->N;
+  a.nq = e->nq;
+  a.Q = e->Q;
+  a.G = e->G;
+  a.epi = epi;
+  a.max_split = e->G;
+  a.min_split = e->min_split;
+  a.clampv = e->cfg.clamp;
+  LayerKernelKey k = e->key;
+  k.constw = d.constw;
+  CK(launch_layer(k, a, e->grid, e->threads, e->smem, e->stream));
+  e->launches++;
+  return SDNN_OK;
+}
+
+int record(sdnn_engine* e, int i, bool capturing) {
+  if (capturing) {
+    CK(cudaEventRecordWithFlags(e->ev[i], e->stream, cudaEventRecordExternal));
+  } else {
+    CK(cudaEventRecord(e->ev[i], e->stream));
+  }
+  return SDNN_OK;
+}
+
+int effective_threshold(const sdnn_engine* e) {
+  if (e->cfg.mode != SDNN_MODE_SNICIT) return e->L;
+  return std::max(0, std::min(e->cfg.threshold, e->L));
+}
+
+// Enqueues one inference of `rows` rows read from d_in, flags to d_flags.
+int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, bool capturing) {
+  const int L = e->L;
+  const int T = effective_threshold(e);
+  const size_t N = (size_t)e->N;
+  const cudaStream_t s = e->stream;
+  e->launches = 0;
+  int rc;
+  if ((rc = record(e, 0, capturing))) return rc;
+  CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
+  CK(cudaMemsetAsync(d_flags, 0, (size_t)rows * 4, s));
+  CK(cudaMemsetAsync(e->d_state, 0, (size_t)rows * 4, s));
+  launch_iota(e->d_list[0], e->d_counts, (int32_t)rows, s);
+  e->launches++;
+  // XY mode splits the plain loop at the threshold for its pre/post timing
+  // (src/SDGC/XY/XY.hpp:492-501); BF and SNIG time the loop as one stage.
+  const int split = e->cfg.mode == SDNN_MODE_XY ? std::max(0, std::min(e->cfg.threshold, L)) : T;
+  for (int l = 0; l < T; ++l) {
+    if (l == split && T == L) {
+      if ((rc = record(e, 1, capturing))) return rc;
+      if ((rc = record(e, 2, capturing))) return rc;
+    }
+    const float* in = l == 0 ? d_in : e->d_y[(l - 1) & 1];
+    if ((rc = layer_launch(e, l, EPI_PLAIN, in, e->d_y[l & 1], e->d_list[l & 1], e->d_counts + l,
+                           e->d_list[(l + 1) & 1], e->d_counts + l + 1)))
+      return rc;
+  }
+  if (!(split < T && T == L)) {
+    if ((rc = record(e, 1, capturing))) return rc;
+  }
+  if (T < L) {
+    float* ybuf = e->d_y[(T - 1 + 2) & 1];
+    if (T == 0) CK(cudaMemcpyAsync(ybuf, d_in, (size_t)rows * N * 4, cudaMemcpyDeviceToDevice, s));
+    const int32_t* live = e->d_list[T & 1];
+    const int32_t* live_count = e->d_counts + T;
+    CK(cudaMemsetAsync(e->d_rcounts, 0, (size_t)(L + 4) * 4, s));
+    CK(cudaMemsetAsync(e->d_iscent, 0, (size_t)rows * 4, s));
+    CK(cudaMemsetAsync(e->d_resflag, 0, (size_t)rows * 4, s));
+    CK(cudaMemsetAsync(e->d_ccount, 0, 16, s));
+    CK(cudaMemsetAsync(e->d_ncand, 0, 16, s));
+    ClusterArgs c{};
+    c.y = ybuf;
+    c.live = live;
+    c.live_count = live_count;
+    c.N = e->N;
+    c.K = e->Kmax;
+    c.seed = e->cfg.seed;
+    c.cand = e->d_cand;
+    c.ncand = e->d_ncand;
+    c.bins = e->d_bins;
+    c.clist = e->d_clist;
+    c.ccount = e->d_ccount;
+    c.cslot = e->d_cslot;
+    c.rlist = e->d_rlist[0];
+    c.rcount = e->d_rcounts;
+    c.is_centroid = e->d_iscent;
+    c.err = e->d_err;
+    launch_cluster(c, e->num_sms, s);
+    e->launches += 4;
+    if ((rc = record(e, 2, capturing))) return rc;
+    for (int l = T; l < L; ++l) {
+      const int p = l - T;
+      const float* in = e->d_y[(l - 1 + 2) & 1];
+      float* out = e->d_y[l & 1];
+      if ((rc = layer_launch(e, l, EPI_CENTROID, in, out, e->d_clist, e->d_ccount, nullptr,
+                             nullptr)))
+        return rc;
+      if ((rc = layer_launch(e, l, EPI_RESIDUE, in, out, e->d_rlist[p & 1], e->d_rcounts + p,
+                             e->d_rlist[(p + 1) & 1], e->d_rcounts + p + 1)))
+        return rc;
+    }
+    if ((rc = record(e, 3, capturing))) return rc;
+    const int pf = L - T;
+    launch_mark_rows(e->d_rlist[pf & 1], e->d_rcounts + pf, e->d_resflag, 1, s);
+    launch_recover(e->d_y[(L - 1) & 1], live, live_count, e->d_cslot, e->d_clist, e->d_iscent,
+                   e->d_resflag, e->N, d_flags, s);
+    launch_mark_rows(live, live_count, e->d_state, 2, s);
+    e->launches += 3;
+  } else {
+    if (!(split < T)) {
+      if ((rc = record(e, 2, capturing))) return rc;
+    }
+    if ((rc = record(e, 3, capturing))) return rc;
+    launch_identify(e->d_y[(L - 1) & 1], e->d_list[L & 1], e->d_counts + L, e->N, d_flags, s);
+    launch_mark_rows(e->d_list[L & 1], e->d_counts + L, e->d_state, 1, s);
+    e->launches += 2;
+  }
+  if ((rc = record(e, 4, capturing))) return rc;
+  CK(cudaGetLastError());
+  return SDNN_OK;
+}
+
+int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
+  if (rows <= 0) return fail(e, SDNN_ERR_INVALID, "rows must be positive");
+  if (rows > e->cap) return fail(e, SDNN_ERR_INVALID, "rows exceed the batch capacity");
+  const bool graph = e->cfg.mode != SDNN_MODE_BF;
+  const int T = effective_threshold(e);
+  e->last_T = T;
+  e->last_rows = rows;
+  if (!graph) {
+    int rc = enqueue(e, rows, d_in, d_flags, false);
+    if (rc) return rc;
+  } else {
+    if (!e->gexec || e->g_rows != rows || e->g_in != d_in || e->g_flags != d_flags ||
+        e->g_T != T || e->g_K != e->Kmax || e->g_mode != e->cfg.mode ||
+        e->g_tile != e->key.T || e->g_threads != e->threads) {
+      drop_graph(e);
+      CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = enqueue(e, rows, d_in, d_flags, true);
+      cudaGraph_t g = nullptr;
+      cudaError_t rc2 = cudaStreamEndCapture(e->stream, &g);
+      if (rc != SDNN_OK) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc;
+      }
+      if (rc2 != cudaSuccess) return cuda_fail(e, rc2, "cudaStreamEndCapture");
+      cudaError_t rc3 = cudaGraphInstantiate(&e->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (rc3 != cudaSuccess) {
+        e->gexec = nullptr;
+        return cuda_fail(e, rc3, "cudaGraphInstantiate");
+      }
+      e->g_rows = rows;
+      e->g_in = d_in;
+      e->g_flags = d_flags;
+      e->g_T = T;
+      e->g_K = e->Kmax;
+      e->g_mode = e->cfg.mode;
+      e->g_tile = e->key.T;
+      e->g_threads = e->threads;
+    }
+    CK(cudaGraphLaunch(e->gexec, e->stream));
+  }
+  e->have_run = true;
+  e->pending_stats = 1;
+  return SDNN_OK;
+}
+
+int ensure_cuda(sdnn_engine* e) {
+  if (e->stream) {
+    CK(cudaSetDevice(e->dev));
+    return SDNN_OK;
+  }
+  CK(cudaSetDevice(e->dev));
+  CK(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, e->dev));
+  CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  for (int i = 0; i < 5; ++i) CK(cudaEventCreate(&e->ev[i]));
+  return SDNN_OK;
+}
+
+int prepare(sdnn_engine* e, int64_t rows) {
+  int rc = ensure_cuda(e);
+  if (rc) return rc;
+  rc = finalize_weights(e);
+  if (rc) return rc;
+  if (e->grid == 0) {
+    rc = choose_kernel(e);
+    if (rc) return rc;
+  }
+  CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, true}, e->smem));
+  CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
+  return ensure_buffers(e, rows);
+}
+
+int check_device_error(sdnn_engine* e) {
+  int32_t h = 0;
+  CK(cudaMemcpyAsync(&h, e->d_err, 4, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  if (h == DEV_TIMEOUT) {
+    cudaMemsetAsync(e->d_err, 0, 4, e->stream);
+    cudaMemsetAsync(e->d_tmask, 0, (size_t)(e->cap + 1) * 4, e->stream);
+    cudaMemsetAsync(e->d_ticket, 0, (size_t)(e->cap + 1) * 4, e->stream);
+    return fail(e, SDNN_ERR_TIMEOUT, "a device-side wait timed out");
+  }
+  if (h != 0) return fail(e, SDNN_ERR_CUDA, "device error word " + std::to_string(h));
+  return SDNN_OK;
+}
+
+int collect_stats(sdnn_engine* e) {
+  if (!e->pending_stats) return SDNN_OK;
+  CK(cudaStreamSynchronize(e->stream));
+  const int L = e->L, T = e->last_T;
+  std::vector<int32_t> counts(L + 4), rcounts(L + 4);
+  int32_t ccount = 0;
+  CK(cudaMemcpy(counts.data(), e->d_counts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
+  sdnn_stats& st = e->stats;
+  std::memset(&st, 0, sizeof(st));
+  float ms[4] = {0, 0, 0, 0};
+  for (int i = 0; i < 4; ++i) CK(cudaEventElapsedTime(&ms[i], e->ev[i], e->ev[i + 1]));
+  // ev1->ev2 covers the clustering, ev2->ev3 the post layers
+  for (int i = 0; i < 4; ++i) st.stage_ms[i] = ms[i];
+  CK(cudaEventElapsedTime(&st.total_ms, e->ev[0], e->ev[4]));
+  st.rows_in = e->last_rows;
+  int64_t pre = 0, post = 0;
+  for (int l = 0; l < T; ++l) pre += counts[l];
+  if (T < L) {
+    CK(cudaMemcpy(rcounts.data(), e->d_rcounts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ccount, e->d_ccount, 4, cudaMemcpyDeviceToHost));
+    for (int p = 0; p < L - T; ++p) post += ccount + rcounts[p];
+    st.centroids = ccount;
+    st.residue_rows = rcounts[0];
+    st.rows_out = 0;
+  } else {
+    st.rows_out = counts[L];
+  }
+  st.pre_row_layers = pre;
+  st.post_row_layers = post;
+  st.row_layers = pre + post;
+  st.weight_nnz = e->total_nnz;
+  st.launches = e->launches;
+  st.threshold = T;
+  st.tile_rows = e->key.T;
+  st.threads = e->threads;
+  e->pending_stats = 0;
+  return SDNN_OK;
+}
+
+}  // namespace
+
+// ============================================================== C ABI
+
+extern "C" {
+
+int sdnn_abi_version(void) { return SDNN_ABI_VERSION; }
+
+const char* sdnn_status_string(int status) {
+  switch (status) {
+    case SDNN_OK: return "ok";
+    case SDNN_ERR_INVALID: return "invalid argument";
+    case SDNN_ERR_CUDA: return "CUDA error";
+    case SDNN_ERR_OOM: return "out of memory";
+    case SDNN_ERR_IO: return "I/O error";
+    case SDNN_ERR_FORMAT: return "malformed input";
+    case SDNN_ERR_STATE: return "call out of order";
+    case SDNN_ERR_TIMEOUT: return "device wait timed out";
+    case SDNN_ERR_UNSUPPORTED: return "unsupported";
+    case SDNN_ERR_BUSY: return "busy";
+    default: return "unknown status";
+  }
+}
+
+float sdnn_reference_bias(int32_t n) {
+  switch (n) {
+    case 65536: return -0.45f;
+    case 16384: return -0.4f;
+    case 4096: return -0.35f;
+    case 1024: return -0.3f;
+    default: return 0.f;
+  }
+}
+
+int sdnn_config_default(sdnn_config* c) {
+  if (!c) return SDNN_ERR_INVALID;
+  std::memset(c, 0, sizeof(*c));
+  c->num_neurons = 1024;
+  c->num_layers = 120;
+  c->mode = SDNN_MODE_SNICIT;
+  c->threshold = 30;
+  c->batch = 60000;
+  c->bias = sdnn_reference_bias(1024);
+  c->clamp = 32.f;
+  c->num_centroids = 32;
+  c->autotune = 0;
+  c->seed = 20260101ull;
+  c->device = 0;
+  return SDNN_OK;
+}
+
+int sdnn_create(const sdnn_config* cfg, sdnn_engine** out) {
+  if (!cfg || !out) return SDNN_ERR_INVALID;
+  *out = nullptr;
+  if (cfg->num_neurons < 32 || cfg->num_neurons % 32 != 0) return SDNN_ERR_INVALID;
+  if (cfg->num_neurons > 32768 && cfg->num_neurons % 16384 != 0) return SDNN_ERR_INVALID;
+  if (cfg->num_layers < 1 || cfg->batch < 1 || cfg->batch > (int64_t)1 << 30) return SDNN_ERR_INVALID;
+  if (cfg->mode < SDNN_MODE_BF || cfg->mode > SDNN_MODE_SNICIT) return SDNN_ERR_INVALID;
+  if (cfg->num_centroids < 1 || cfg->num_centroids > 256) return SDNN_ERR_INVALID;
+  if (!(cfg->clamp > 0.f)) return SDNN_ERR_INVALID;
+  if (cfg->tile_rows < 0 || cfg->tile_rows > 32) return SDNN_ERR_INVALID;
+  auto* e = new (std::nothrow) sdnn_engine();
+  if (!e) return SDNN_ERR_OOM;
+  e->cfg = *cfg;
+  e->N = cfg->num_neurons;
+  e->L = cfg->num_layers;
+  e->dev = cfg->device;
+  e->hw.resize(e->L);
+  // CUDA is initialised on first device use (ensure_cuda), so weights can be
+  // loaded, generated and written on a host without a GPU.
+  *out = e;
+  return SDNN_OK;
+}
+
+int sdnn_destroy(sdnn_engine* e) {
+  if (!e) return SDNN_OK;
+  if (e->stream) {
+    cudaSetDevice(e->dev);
+    cudaStreamSynchronize(e->stream);
+  }
+  drop_graph(e);
+  free_weights(e);
+  free_buffers(e);
+  for (auto& ev : e->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return SDNN_OK;
+}
+
+const char* sdnn_last_error(const sdnn_engine* e) { return e ? e->err.c_str() : ""; }
+
+int sdnn_load_weights_tsv(sdnn_engine* e, const char* dir) {
+  if (!e || !dir) return SDNN_ERR_INVALID;
+  e->gen.on = false;
+  for (int l = 0; l < e->L; ++l) {
+    const std::string p = std::string(dir) + "/n" + std::to_string(e->N) + "-l" +
+                          std::to_string(l + 1) + ".tsv";
+    int rc = read_weight_tsv(p, e->N, e->hw[l], e->err);
+    if (rc) return rc;
+  }
+  e->weights_dirty = true;
+  return SDNN_OK;
+}
+
+int sdnn_set_layer_coo(sdnn_engine* e, int32_t layer, const int32_t* rows, const int32_t* cols,
+                       const float* vals, int64_t nnz) {
+  if (!e) return SDNN_ERR_INVALID;
+  if (layer < 0 || layer >= e->L || nnz < 0 || (nnz > 0 && (!rows || !cols || !vals)))
+    return fail(e, SDNN_ERR_INVALID, "bad layer or arrays");
+  if (e->gen.on) {
+    // switching from generated to explicit weights: materialise the others
+    e->gen.on = false;
+    for (auto& h : e->hw) h.present = false;
+  }
+  if (!coo_to_host_layer(e->N, rows, cols, vals, nnz, e->hw[layer], e->err)) return SDNN_ERR_INVALID;
+  e->weights_dirty = true;
+  return SDNN_OK;
+}
+
+int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias) {
+  if (!e || !bias) return SDNN_ERR_INVALID;
+  if (layer < 0 || layer >= e->L) return fail(e, SDNN_ERR_INVALID, "bad layer");
+  if ((int)e->hbias.size() < e->L) e->hbias.resize(e->L);
+  e->hbias[layer].assign(bias, bias + e->N);
+  e->weights_dirty = true;
+  return SDNN_OK;
+}
+
+int sdnn_generate_weights(sdnn_engine* e, uint64_t seed, int32_t nnz_per_row, float value) {
+  if (!e) return SDNN_ERR_INVALID;
+  if (nnz_per_row < 1 || nnz_per_row > e->N) return fail(e, SDNN_ERR_INVALID, "bad nnz_per_row");
+  e->gen.on = true;
+  e->gen.seed = seed;
+  e->gen.nnz = nnz_per_row;
+  e->gen.value = value;
+  for (auto& h : e->hw) h = HostLayer{};
+  e->weights_dirty = true;
+  return SDNN_OK;
+}
+
+int sdnn_finalize_weights(sdnn_engine* e) {
+  if (!e) return SDNN_ERR_INVALID;
+  int rc = ensure_cuda(e);
+  if (rc) return rc;
+  return finalize_weights(e);
+}
+
+int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows, int32_t* d_flags,
+                      void* stream) {
+  if (!e || !d_Y0 || !d_flags || rows <= 0) return SDNN_ERR_INVALID;
+  int rc = prepare(e, rows);
+  if (rc) return rc;
+  cudaStream_t user = (cudaStream_t)stream;
+  cudaEvent_t joined = nullptr;
+  if (user && user != e->stream) {
+    // order the engine stream after the caller's stream, then back
+    CK(cudaEventCreateWithFlags(&joined, cudaEventDisableTiming));
+    CK(cudaEventRecord(joined, user));
+    CK(cudaStreamWaitEvent(e->stream, joined, 0));
+  }
+  rc = run(e, rows, d_Y0, d_flags);
+  if (joined) {
+    cudaEventRecord(joined, e->stream);
+    cudaStreamWaitEvent(user, joined, 0);
+    cudaEventDestroy(joined);
+  }
+  return rc;
+}
+
+int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows, int32_t* flags, int32_t* ids,
+                    int64_t* count) {
+  if (!e || !Y0 || rows <= 0) return SDNN_ERR_INVALID;
+  int rc = prepare(e, std::min<int64_t>(rows, e->cfg.batch));
+  if (rc) return rc;
+  const int64_t N = e->N;
+  int64_t total = 0;
+  sdnn_stats acc{};
+  for (int64_t off = 0; off < rows; off += e->cfg.batch) {
+    const int64_t n = std::min<int64_t>(e->cfg.batch, rows - off);
+    CK(cudaMemcpyAsync(e->d_in, Y0 + off * N, (size_t)(n * N) * 4, cudaMemcpyHostToDevice,
+                       e->stream));
+    rc = run(e, n, e->d_in, e->d_flags);
+    if (rc) return rc;
+    if (ids || count) {
+      launch_flags_to_ids(e->d_flags, (int32_t)n, e->d_ids, e->d_idcount, e->stream);
+      int32_t c = 0;
+      CK(cudaMemcpyAsync(&c, e->d_idcount, 4, cudaMemcpyDeviceToHost, e->stream));
+      CK(cudaStreamSynchronize(e->stream));
+      if (ids && c > 0) {
+        CK(cudaMemcpyAsync(ids + total, e->d_ids, (size_t)c * 4, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        for (int32_t i = 0; i < c; ++i) ids[total + i] += (int32_t)off;
+      }
+      total += c;
+    }
+    if (flags)
+      CK(cudaMemcpyAsync(flags + off, e->d_flags, (size_t)n * 4, cudaMemcpyDeviceToHost, e->stream));
+    rc = check_device_error(e);
+    if (rc) return rc;
+    rc = collect_stats(e);
+    if (rc) return rc;
+    for (int i = 0; i < 4; ++i) acc.stage_ms[i] += e->stats.stage_ms[i];
+    acc.total_ms += e->stats.total_ms;
+    acc.rows_in += e->stats.rows_in;
+    acc.row_layers += e->stats.row_layers;
+    acc.pre_row_layers += e->stats.pre_row_layers;
+    acc.post_row_layers += e->stats.post_row_layers;
+    acc.weight_nnz = e->stats.weight_nnz;
+    acc.centroids = e->stats.centroids;
+    acc.residue_rows += e->stats.residue_rows;
+    acc.launches += e->stats.launches;
+    acc.threshold = e->stats.threshold;
+    acc.tile_rows = e->stats.tile_rows;
+    acc.threads = e->stats.threads;
+  }
+  acc.rows_out = total;
+  e->stats = acc;
+  if (count) *count = total;
+  return SDNN_OK;
+}
+
+int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows) {
+  if (!e || !out) return SDNN_ERR_INVALID;
+  if (!e->have_run) return fail(e, SDNN_ERR_STATE, "no inference has run");
+  if (rows != e->last_rows) return fail(e, SDNN_ERR_INVALID, "rows differ from the last batch");
+  cudaSetDevice(e->dev);
+  const int L = e->L;
+  float* scratch = e->d_y[L & 1];
+  launch_materialize(e->d_y[(L - 1) & 1], e->d_state, e->d_cslot, e->d_clist, e->d_iscent,
+                     e->d_resflag, e->N, scratch, (int32_t)rows, e->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, scratch, (size_t)rows * e->N * 4, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  // the scratch buffer is the next inference's layer buffer; nothing to restore
+  return SDNN_OK;
+}
+
+int sdnn_get_stats(const sdnn_engine* ce, sdnn_stats* out) {
+  if (!ce || !out) return SDNN_ERR_INVALID;
+  auto* e = const_cast<sdnn_engine*>(ce);
+  if (e->pending_stats) {
+    cudaSetDevice(e->dev);
+    int rc = collect_stats(e);
+    if (rc) return rc;
+  }
+  *out = e->stats;
+  return SDNN_OK;
+}
+
+int sdnn_write_weights_tsv(sdnn_engine* e, const char* dir) {
+  if (!e || !dir) return SDNN_ERR_INVALID;
+  for (int l = 0; l < e->L; ++l) {
+    HostLayer tmp;
+    const HostLayer* h = &e->hw[l];
+    if (e->gen.on) {
+      const int N = e->N, k = e->gen.nnz;
+      tmp.row_off.resize(N + 1);
+      tmp.cols.resize((size_t)N * k);
+      tmp.vals.assign((size_t)N * k, e->gen.value);
+      for (int j = 0; j < N; ++j) {
+        tmp.row_off[j] = j * k;
+        int32_t* c = tmp.cols.data() + (size_t)j * k;
+        gen_row_cols(e->gen.seed, l, j, N, k, c);
+        std::sort(c, c + k);
+      }
+      tmp.row_off[N] = N * k;
+      h = &tmp;
+    } else if (!h->present) {
+      return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
+    }
+    const std::string p =
+        std::string(dir) + "/n" + std::to_string(e->N) + "-l" + std::to_string(l + 1) + ".tsv";
+    int rc = write_weight_tsv(p, *h, e->N);
+    if (rc) return fail(e, rc, "cannot write " + p);
+  }
+  return SDNN_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- internal hooks
+
+// Used by the autotuner (autotune.cpp).
+namespace sdnn {
+int engine_set_tile(sdnn_engine* e, int tile_rows, int threads) {
+  e->cfg.tile_rows = tile_rows;
+  e->cfg.threads = threads;
+  e->grid = 0;
+  drop_graph(e);
+  return choose_kernel(e);
+}
+void engine_set_snicit(sdnn_engine* e, int threshold, int centroids) {
+  e->cfg.threshold = threshold;
+  if (centroids != e->cfg.num_centroids) {
+    e->cfg.num_centroids = centroids;
+    free_buffers(e);
+  }
+  drop_graph(e);
+}
+sdnn_config engine_config(const sdnn_engine* e) { return e->cfg; }
+}  // namespace sdnn

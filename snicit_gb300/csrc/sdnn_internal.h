@@ -1,0 +1,117 @@
+// Internal declarations shared by the kernel translation units and the engine.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sdnn {
+
+// Epilogue variants of the layer kernel.
+//  PLAIN     y = clamp(acc + b)                       (bf_inference, src/SDGC/BF/kernel.hpp:76-85)
+//  CENTROID  pre = acc + b stored; y = clamp(pre)     (post_minus centroid branch,
+//                                                      src/SDGC/SNICIT/kernel.hpp:114-120)
+//  RESIDUE   y = clamp(pre_c + acc) - clamp(pre_c)    (post_minus residue branch,
+//                                                      src/SDGC/SNICIT/kernel.hpp:121-135)
+enum Epilogue : int32_t { EPI_PLAIN = 0, EPI_CENTROID = 1, EPI_RESIDUE = 2 };
+
+// Device error codes written to the engine's error word (0 = ok).
+enum DevError : int32_t { DEV_OK = 0, DEV_TIMEOUT = 7, DEV_BAD_ROW = 1 };
+
+// Bank-scheduled layer layout.  Outputs are taken in groups of 32 (lane i of
+// the group computes output 32*g + i).  For every (group, input chunk) the
+// in-edges are arranged in "slots": one edge per lane per slot, and the 32
+// input indices of a slot fall in 32 distinct shared-memory banks.  Slots are
+// stored in blocks of 4: block b holds, for each lane, 4 consecutive uint16
+// chunk-local indices (one uint2) and, unless the layer has one common value,
+// 4 floats (one float4).  Empty lanes point at a zero column (chunk + bank).
+struct LayerDev {
+  const uint2* idx;        // [blocks][32] uint2 (4 x u16)
+  const float4* val;       // [blocks][32] float4, nullptr when const_w
+  const int32_t* grp_blk;  // [G*nq + 1] block offsets, entry g*nq + q
+  const float* bias_vec;   // [N] per-neuron bias or nullptr
+  float bias;              // scalar bias when bias_vec == nullptr
+  float wconst;            // common value when val == nullptr
+};
+
+struct LayerArgs {
+  LayerDev w;
+  const float* y_in;        // [rows][N]
+  float* y_out;             // [rows][N]
+  const int32_t* list_in;   // row ids to process
+  const int32_t* count_in;  // number of ids (device scalar)
+  int32_t* list_out;        // surviving ids (PLAIN) / non-empty residues (RESIDUE)
+  int32_t* count_out;       // device scalar, must start at 0
+  uint32_t* tile_mask;      // scratch per tile, zero between launches
+  int32_t* tile_ticket;     // scratch per tile, zero between launches
+  float* pre_out;           // CENTROID: [K][N] pre-activations
+  const float* pre_in;      // RESIDUE:  [K][N] pre-activations of this layer
+  const int32_t* cslot;     // row -> centroid slot
+  int32_t* err;             // device error word
+  int32_t N, nq, Q, G;
+  int32_t epi;
+  int32_t max_split;        // upper bound of CTAs sharing one tile
+  int32_t min_split;        // lower bound (register capacity of chunked kernels)
+  float clampv;
+};
+
+// Kernel instance selection.
+struct LayerKernelKey {
+  int T;       // rows per tile
+  int rsw;     // compile-time smem row stride in floats (0 = runtime)
+  int kg;      // groups per warp held across chunks (1 = no chunking)
+  bool constw;
+};
+
+// Launches the layer kernel instance matching key; returns cudaErrorInvalidValue
+// if no instance exists.  grid/threads/smem chosen by the caller.
+cudaError_t launch_layer(const LayerKernelKey& key, const LayerArgs& a, int grid, int threads,
+                         size_t smem, cudaStream_t s);
+// Occupancy query for an instance (blocks per SM), 0 if not available.
+int layer_blocks_per_sm(const LayerKernelKey& key, int threads, size_t smem);
+// True if an instance exists.
+bool layer_instance_exists(const LayerKernelKey& key);
+// Sets the max dynamic shared memory attribute of an instance.
+cudaError_t layer_prepare(const LayerKernelKey& key, size_t smem);
+
+// ---- auxiliary kernels (aux.cu) ----
+void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);
+void launch_identify(const float* y, const int32_t* list, const int32_t* count, int32_t N,
+                     int32_t* flags, cudaStream_t s);
+void launch_flags_to_ids(const int32_t* flags, int32_t n, int32_t* ids, int32_t* count,
+                         cudaStream_t s);
+void launch_mark_rows(const int32_t* list, const int32_t* count, int32_t* flags, int32_t value,
+                      cudaStream_t s);
+
+// SNICIT threshold stage.
+struct ClusterArgs {
+  float* y;                 // [rows][N] activations at the threshold, rewritten to residues
+  const int32_t* live;      // live rows at the threshold
+  const int32_t* live_count;
+  int32_t N;
+  int32_t K;                // candidate count
+  uint64_t seed;
+  int32_t* cand;            // [K] candidate rows (seeded pick)
+  int32_t* ncand;
+  float* bins;              // [K][16] downsampled sums
+  int32_t* clist;           // [K] kept centroid rows
+  int32_t* ccount;
+  int32_t* cslot;           // [rows] centroid slot of every live row
+  int32_t* rlist;           // non-empty residue rows
+  int32_t* rcount;
+  int32_t* is_centroid;     // [rows] 1 for centroid rows
+  int32_t* err;
+};
+void launch_cluster(const ClusterArgs& a, int num_sms, cudaStream_t s);
+
+// Recovery (SNICIT.hpp:644 recover): flags[r] = any(c + delta > 0) for every
+// live row at the threshold; rows absent from the final residue list have
+// delta == 0.
+void launch_recover(const float* y, const int32_t* live, const int32_t* live_count,
+                    const int32_t* cslot, const int32_t* clist, const int32_t* is_centroid,
+                    const int32_t* res_flag, int32_t N, int32_t* flags, cudaStream_t s);
+// Final activations of every row into out[rows][N]: state 0 = dead (zeros),
+// 1 = plain final row, 2 = SNICIT live row (centroid, or centroid + residue).
+void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
+                        const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
+                        int32_t N, float* out, int32_t rows, cudaStream_t s);
+
+}  // namespace sdnn

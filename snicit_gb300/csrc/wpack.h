@@ -1,0 +1,42 @@
+// Host-side weight storage and the bank-scheduled packer.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace sdnn {
+
+// One layer as CSR by input row (row = input neuron j, col = output neuron c),
+// duplicates summed in input order, columns ascending within a row.  This is
+// the content of the reference's packed per-layer CSR
+// (tsv_string_to_CSR_packed_array, src/SDGC/utility.hpp:85-126) without the
+// N_SLAB section folding.
+struct HostLayer {
+  std::vector<int32_t> row_off;  // N + 1
+  std::vector<int32_t> cols;
+  std::vector<float> vals;
+  bool present = false;
+};
+
+// Builds a HostLayer from COO triplets (0-based); duplicates are summed in
+// the order given.  Returns false on out-of-range indices.
+bool coo_to_host_layer(int32_t N, const int32_t* rows, const int32_t* cols, const float* vals,
+                       int64_t nnz, HostLayer& out, std::string& err);
+
+// Packed layer (see LayerDev in sdnn_internal.h).
+struct PackedLayer {
+  std::vector<uint16_t> idx;     // nblocks * 32 * 4
+  std::vector<float> val;        // nblocks * 32 * 4 (empty when constw)
+  std::vector<int32_t> grp_blk;  // G*nq + 1
+  bool constw = true;
+  float wconst = 0.f;
+  int64_t nblocks = 0;
+  int64_t nnz = 0;
+  int32_t max_depth = 0;         // deepest slot list of a (group, chunk)
+  int64_t slots = 0;             // total slots (sum of depths)
+};
+
+// Packs one layer for chunk size Q (N % Q == 0, Q % 32 == 0, Q + 32 <= 65536).
+void pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out);
+
+}  // namespace sdnn

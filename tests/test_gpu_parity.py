@@ -1,0 +1,237 @@
+"""GPU parity of the CUDA path against the FP64 oracle (through the C ABI).
+
+Tolerances (stated by the benchmark spec): the category set is bit-exact; final
+activations agree with the FP64 oracle within 1e-5 relative, measured as
+|gpu - ref| / max(1, |ref|) (activations live in [0, 32]).
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import snicit_gb300 as sg
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-5
+
+
+def _layers(N, L, seed, nnz=32, value=0.0625):
+    return [sg.generate_layer_csr(N, seed, l, nnz, value) for l in range(L)]
+
+
+def _check(Y, flags, ids, Yref, alive, label):
+    want = np.flatnonzero(alive)
+    assert np.array_equal(ids, want), f"{label}: category set differs ({len(ids)} vs {len(want)})"
+    assert np.array_equal(flags, alive.astype(np.int32)), f"{label}: flags differ"
+    err = np.abs(Y.astype(np.float64) - Yref) / np.maximum(1.0, np.abs(Yref))
+    assert err.max() <= RTOL, f"{label}: activation error {err.max():.3g}"
+
+
+def _run(N, L, B, seed, mode, threshold=30, bias=None, centroids=32, tile_rows=0, threads=0,
+         batch=None, Y0=None, weights=None):
+    bias = sg.load().sdnn_reference_bias(N) if bias is None else bias
+    if bias == 0.0:
+        bias = -0.3
+    Y0 = sg.generate_inputs(N, seed, 0, B) if Y0 is None else Y0
+    with sg.Engine(N, L, mode=mode, threshold=threshold, batch=batch or B, bias=bias,
+                   num_centroids=centroids, tile_rows=tile_rows, threads=threads) as eng:
+        if weights is None:
+            eng.generate_weights(seed)
+        else:
+            for l, (ro, c, v) in enumerate(weights):
+                eng.set_layer_csr(l, ro, c, v)
+        flags, ids = eng.infer(Y0)
+        Y = eng.activations(B) if (batch is None or batch >= B) else None
+        st = eng.stats()
+    return Y0, flags, ids, Y, st, bias
+
+
+@pytest.mark.parametrize("mode", ["BF", "SNIG", "XY"])
+@pytest.mark.parametrize("N,L,B", [(256, 20, 300), (1024, 24, 200), (4096, 12, 64)])
+def test_plain_modes(mode, N, L, B):
+    seed = 100 + N + L
+    Y0, flags, ids, Y, st, bias = _run(N, L, B, seed, mode, threshold=L // 2)
+    Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+    _check(Y, flags, ids, Yref, alive, f"{mode} N={N}")
+    assert st["rows_out"] == len(ids)
+
+
+@pytest.mark.parametrize("N,L,B,T,K", [(1024, 40, 400, 8, 32), (1024, 40, 400, 1, 4),
+                                       (4096, 24, 96, 6, 16), (256, 30, 500, 12, 50)])
+def test_snicit_matches_oracle(N, L, B, T, K):
+    seed = 7 + N + T
+    Y0, flags, ids, Y, st, bias = _run(N, L, B, seed, "SNICIT", threshold=T, centroids=K)
+    layers = _layers(N, L, seed)
+    Yref, alive, _ = orc.infer(layers, N, bias, Y0, precision=64)
+    _check(Y, flags, ids, Yref, alive, f"SNICIT N={N} t={T}")
+    assert st["threshold"] == T and st["centroids"] >= 1
+
+
+def test_snicit_residue_form_oracle_agrees():
+    """The FP64 residue-form restatement gives the plain categories (exactness)."""
+    N, L, B, T, seed = 256, 24, 300, 4, 5
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    layers = _layers(N, L, seed)
+    Yref, alive, dead = orc.infer(layers, N, -0.3, Y0, precision=64)
+    Yt, alive_t, _ = orc.infer(layers[:T], N, -0.3, Y0, precision=64)
+    live = np.flatnonzero(alive_t)
+    cands = live[orc.ref_candidates(Yt[live].astype(np.float32))]
+    Ys, flags, _, nonempty = orc.snicit(layers, N, -0.3, Y0, T, cands)
+    assert np.array_equal(flags, alive)
+    assert np.abs(Ys - Yref).max() <= 1e-9
+
+
+@pytest.mark.parametrize("mode", ["SNIG", "SNICIT"])
+def test_edge_cases(mode):
+    N, L, seed = 1024, 12, 21
+    # one row; zero rows; rows not a multiple of the tile; all-dead batch
+    for B in (1, 33, 65):
+        Y0 = sg.generate_inputs(N, seed, 0, B)
+        Y0[0] = 0.0
+        _, flags, ids, Y, _, bias = _run(N, L, B, seed, mode, threshold=3, Y0=Y0)
+        Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+        _check(Y, flags, ids, Yref, alive, f"{mode} B={B}")
+        assert flags[0] == 0
+    Y0 = np.zeros((17, N), np.float32)
+    _, flags, ids, Y, _, _ = _run(N, L, 17, seed, mode, threshold=3, Y0=Y0)
+    assert len(ids) == 0 and not flags.any() and not Y.any()
+
+
+@pytest.mark.parametrize("T", [0, 1, 11, 12, 50])
+def test_snicit_threshold_extremes(T):
+    N, L, B, seed = 1024, 12, 150, 33
+    Y0, flags, ids, Y, st, bias = _run(N, L, B, seed, "SNICIT", threshold=T)
+    Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+    _check(Y, flags, ids, Yref, alive, f"t={T}")
+    assert st["threshold"] == min(T, L)
+
+
+def test_single_layer_and_single_centroid():
+    N, B, seed = 1024, 80, 3
+    for L, T, K in ((1, 0, 1), (2, 1, 1), (5, 2, 1)):
+        Y0, flags, ids, Y, _, bias = _run(N, L, B, seed, "SNICIT", threshold=T, centroids=K)
+        Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+        _check(Y, flags, ids, Yref, alive, f"L={L}")
+
+
+def test_general_weights_per_neuron_bias():
+    """beyond-shaped layers: random-valued sparse W, per-neuron bias, clamp 32."""
+    N, L, B = 1024, 10, 128
+    rng = np.random.default_rng(9)
+    layers, biases = [], []
+    for _ in range(L):
+        mask = rng.random((N, N)) < 0.03
+        r, c = np.nonzero(mask)
+        v = (rng.standard_normal(len(r)) * 0.3).astype(np.float32)
+        layers.append(sg.coo_to_csr(N, r, c, v))
+        biases.append(rng.uniform(-0.1, 0.0, N).astype(np.float32))
+    Y0 = rng.random((B, N)).astype(np.float32)
+    for mode in ("SNIG", "SNICIT"):
+        with sg.Engine(N, L, mode=mode, threshold=4, batch=B, bias=-0.05, num_centroids=16) as eng:
+            for l, (ro, c, v) in enumerate(layers):
+                eng.set_layer_csr(l, ro, c, v)
+                eng.set_layer_bias(l, biases[l])
+            flags, ids = eng.infer(Y0)
+            Y = eng.activations(B)
+        Yref, alive, _ = orc.infer(layers, N, -0.05, Y0, precision=64, bias_vec=np.stack(biases))
+        want = np.flatnonzero(alive)
+        assert np.array_equal(ids, want), mode
+        err = np.abs(Y.astype(np.float64) - Yref) / np.maximum(1.0, np.abs(Yref))
+        # general weights: FMA accumulation in a different order than the oracle;
+        # the FP32 rounding of 10 layers of ~31-term sums stays well below this bound
+        assert err.max() <= 1e-4, f"{mode}: {err.max():.3g}"
+
+
+def test_multi_batch_and_determinism():
+    N, L, B, seed = 1024, 16, 500, 44
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    _, f1, ids1, _, _, bias = _run(N, L, B, seed, "SNICIT", threshold=4, batch=128, Y0=Y0)
+    _, f2, ids2, Y2, _, _ = _run(N, L, B, seed, "SNICIT", threshold=4, Y0=Y0)
+    _, f3, ids3, Y3, _, _ = _run(N, L, B, seed, "SNICIT", threshold=4, Y0=Y0)
+    Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+    assert np.array_equal(ids1, np.flatnonzero(alive))
+    assert np.array_equal(ids1, ids2) and np.array_equal(f1, f2)
+    assert np.array_equal(Y2.view(np.uint32), Y3.view(np.uint32)), "runs are not bitwise identical"
+
+
+@pytest.mark.parametrize("tile_rows,threads", [(8, 256), (16, 512), (24, 256), (32, 512)])
+def test_tile_shapes(tile_rows, threads):
+    N, L, B, seed = 1024, 10, 257, 8
+    Y0, flags, ids, Y, st, bias = _run(N, L, B, seed, "SNICIT", threshold=3, tile_rows=tile_rows,
+                                       threads=threads)
+    Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+    _check(Y, flags, ids, Yref, alive, f"T={tile_rows}")
+    assert st["tile_rows"] == tile_rows and st["threads"] == threads
+
+
+@pytest.mark.parametrize("N,L,B", [(16384, 4, 24), (512, 10, 100), (2048, 6, 50)])
+def test_other_widths(N, L, B):
+    seed = 61
+    Y0, flags, ids, Y, st, bias = _run(N, L, B, seed, "SNICIT", threshold=2, bias=-0.4)
+    Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+    _check(Y, flags, ids, Yref, alive, f"N={N}")
+
+
+def test_chunked_width_65536():
+    N, L, B, seed = 65536, 2, 6, 62
+    Y0, flags, ids, Y, st, bias = _run(N, L, B, seed, "SNIG", bias=-0.45)
+    Yref, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64)
+    _check(Y, flags, ids, Yref, alive, "N=65536")
+
+
+def test_tsv_round_trip():
+    N, L, B, seed = 1024, 6, 64, 71
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    with tempfile.TemporaryDirectory() as d:
+        with sg.Engine(N, L, mode="SNIG", batch=B) as a:
+            a.generate_weights(seed)
+            a.write_weights_tsv(d)
+            fa, ia = a.infer(Y0)
+        sg.write_inputs_tsv(os.path.join(d, "in.tsv"), Y0)
+        Y1 = sg.read_inputs_tsv(os.path.join(d, "in.tsv"), N, 0, B)
+        assert np.array_equal(Y0, Y1)
+        with sg.Engine(N, L, mode="SNIG", batch=B) as b:
+            b.load_weights_tsv(d)
+            fb, ib = b.infer(Y1)
+        assert np.array_equal(ia, ib) and np.array_equal(fa, fb)
+        # the reference class mirror reads the same files
+        sg.write_categories_tsv(os.path.join(d, "golden.tsv"), ia)
+        ids = sg.SNICIT(d, -0.3, N, L, 2).infer(os.path.join(d, "in.tsv"),
+                                                  os.path.join(d, "golden.tsv"), B, B, verbose=False)
+        assert np.array_equal(ids, ia)
+
+
+def test_device_pointer_path():
+    torch = pytest.importorskip("torch")
+    N, L, B, seed = 1024, 12, 200, 17
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    d_in = torch.from_numpy(Y0).cuda()
+    d_flags = torch.zeros(B, dtype=torch.int32, device="cuda")
+    with sg.Engine(N, L, mode="SNICIT", threshold=3, batch=B) as eng:
+        eng.generate_weights(seed)
+        s = torch.cuda.current_stream()
+        eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr(), s.cuda_stream)
+        torch.cuda.synchronize()
+        flags = d_flags.cpu().numpy()
+    _, alive, _ = orc.infer(_layers(N, L, seed), N, -0.3, Y0, precision=64, want_y=False)
+    assert np.array_equal(flags, alive)
+
+
+def test_autotune_keeps_categories():
+    N, L, B, seed = 1024, 40, 256, 90
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    with tempfile.TemporaryDirectory() as d:
+        rec = os.path.join(d, "tune.jsonl")
+        with sg.Engine(N, L, mode="SNICIT", threshold=30, batch=B) as eng:
+            eng.generate_weights(seed)
+            eng.autotune(Y0, rec)
+            flags, ids = eng.infer(Y0)
+        lines = open(rec).read().strip().splitlines()
+        assert len(lines) >= 4
+        import json
+        surv = {json.loads(x)["survivors"] for x in lines if json.loads(x)["status"] == 0}
+    _, alive, _ = orc.infer(_layers(N, L, seed), N, -0.3, Y0, precision=64, want_y=False)
+    assert surv == {int(alive.sum())}
+    assert np.array_equal(ids, np.flatnonzero(alive))
