@@ -188,11 +188,17 @@ void drop_graph(sdnn_engine* e) {
 constexpr size_t kMaxSmem = 227 * 1024;
 
 // Chooses chunking, kernel instance, tile rows, threads and grid.
-int choose_kernel(sdnn_engine* e) {
+// Input chunking of the weight layout: whole rows up to 32768 neurons, else
+// chunks of 16384 (fixed at creation; the packer and the kernel share it).
+void choose_layout(sdnn_engine* e) {
   const int N = e->N;
   e->Q = N > 32768 ? 16384 : N;
   e->nq = N / e->Q;
   e->G = N / 32;
+}
+
+int choose_kernel(sdnn_engine* e) {
+  const int N = e->N;
   const int req_T = e->cfg.tile_rows;
   int threads = e->cfg.threads > 0 ? e->cfg.threads : 512;
   if (threads != 256 && threads != 512) threads = 512;
@@ -314,7 +320,10 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
     h = &e->hw[l];
   }
   PackedLayer p;
-  pack_layer(*h, e->N, e->Q, p);
+  if (!pack_layer(*h, e->N, e->Q, p)) {
+    err = "bad chunk size for packing";
+    return SDNN_ERR_INVALID;
+  }
   DevLayer d;
   d.constw = p.constw;
   d.wconst = p.wconst;
@@ -727,6 +736,7 @@ int sdnn_create(const sdnn_config* cfg, sdnn_engine** out) {
   e->L = cfg->num_layers;
   e->dev = cfg->device;
   e->hw.resize(e->L);
+  choose_layout(e);
   // CUDA is initialised on first device use (ensure_cuda), so weights can be
   // loaded, generated and written on a host without a GPU.
   *out = e;
@@ -810,6 +820,9 @@ int sdnn_finalize_weights(sdnn_engine* e) {
 int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows, int32_t* d_flags,
                       void* stream) {
   if (!e || !d_Y0 || !d_flags || rows <= 0) return SDNN_ERR_INVALID;
+  // rows are staged with 1-D TMA bulk copies, which need 16-byte aligned sources
+  if (((uintptr_t)d_Y0 & 15u) != 0)
+    return fail(e, SDNN_ERR_INVALID, "d_Y0 must be 16-byte aligned");
   int rc = prepare(e, rows);
   if (rc) return rc;
   cudaStream_t user = (cudaStream_t)stream;

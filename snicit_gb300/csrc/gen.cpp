@@ -19,9 +19,9 @@ static constexpr uint64_t kGolden = 0x9E3779B97F4A7C15ull;
 // Key of stream (kind, a, b) under seed.
 uint64_t stream_key(uint64_t seed, uint64_t kind, uint64_t a, uint64_t b) {
   uint64_t k = finalize64(seed + kGolden);
-  k = finalize64(k ^ (kind * 0xD1B54A32D192ED03ull) + kGolden);
-  k = finalize64(k ^ (a * 0xABC98388FB8FAC03ull) + kGolden);
-  k = finalize64(k ^ (b * 0x8CB92BA72F3D8DD7ull) + kGolden);
+  k = finalize64(k ^ (kind * 0xD1B54A32D192ED03ull + kGolden));
+  k = finalize64(k ^ (a * 0xABC98388FB8FAC03ull + kGolden));
+  k = finalize64(k ^ (b * 0x8CB92BA72F3D8DD7ull + kGolden));
   return k;
 }
 // i-th 64-bit draw of a stream (SplitMix64 output i+1 from state key).

@@ -56,7 +56,6 @@ namespace {
 // Bitset of slot indices, grown on demand.
 struct SlotSet {
   std::vector<uint64_t> w;
-  bool test(int s) const { return (size_t)(s >> 6) < w.size() && ((w[s >> 6] >> (s & 63)) & 1); }
   void set(int s) {
     if ((size_t)(s >> 6) >= w.size()) w.resize((s >> 6) + 1, 0);
     w[s >> 6] |= 1ull << (s & 63);
@@ -67,7 +66,8 @@ struct SlotSet {
 
 }  // namespace
 
-void pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out) {
+bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out) {
+  if (Q <= 0 || Q % 32 != 0 || N % Q != 0 || Q + 32 > 65536) return false;
   const int32_t G = N / 32, nq = N / Q;
   // CSC: in-edges of every output, inputs ascending.
   std::vector<int32_t> indeg(N + 1, 0);
@@ -122,7 +122,6 @@ void pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out) {
           edges.push_back({l, j - lo, cval[cur[l]], -1});
           ++cur[l];
         }
-        (void)lo;
       }
       for (int l = 0; l < 32; ++l) {
         lane_used[l].clear();
@@ -181,6 +180,7 @@ void pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out) {
   }
   out.grp_blk[(size_t)G * nq] = (int32_t)blk;
   out.nblocks = blk;
+  return true;
 }
 
 }  // namespace sdnn

@@ -36,7 +36,8 @@ struct PackedLayer {
   int64_t slots = 0;             // total slots (sum of depths)
 };
 
-// Packs one layer for chunk size Q (N % Q == 0, Q % 32 == 0, Q + 32 <= 65536).
-void pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out);
+// Packs one layer for chunk size Q (N % Q == 0, Q % 32 == 0, Q + 32 <= 65536);
+// returns false when Q violates that.
+bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out);
 
 }  // namespace sdnn
