@@ -70,7 +70,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -199,7 +199,11 @@ def run_ours(args):
 
     d_in = torch.from_numpy(Y0).to(f"cuda:{local}")
     d_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
-    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    # a real (non-default) stream: the engine orders its own stream after it and
+    # makes it wait for the engine, so events recorded here bracket the work
+    stream = torch.cuda.Stream(device=f"cuda:{local}")
+    torch.cuda.set_stream(stream)
 
     def step():
         eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr(), stream.cuda_stream)
@@ -338,13 +342,13 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sdgc-4096x480", choices=sorted(WORKLOADS))
     ap.add_argument("--threshold", type=int, default=None)
     ap.add_argument("--centroids", type=int, default=50)
-    ap.add_argument("--tune-rows", type=int, default=4096)
+    ap.add_argument("--tune-rows", type=int, default=16384)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

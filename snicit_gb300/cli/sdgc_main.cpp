@@ -29,6 +29,12 @@ static bool exists(const std::string& p) {
   return ::stat(p.c_str(), &st) == 0;
 }
 
+// mkdir -p
+static void make_dirs(const std::string& path) {
+  for (size_t i = 1; i <= path.size(); ++i)
+    if (i == path.size() || path[i] == '/') ::mkdir(path.substr(0, i).c_str(), 0755);
+}
+
 static int die(sdnn_engine* e, int rc, const char* what) {
   std::fprintf(stderr, "%s failed: %s (%s)\n", what, sdnn_status_string(rc),
                e ? sdnn_last_error(e) : "");
@@ -105,10 +111,8 @@ int main(int argc, char** argv) {
     rc = sdnn_generate_inputs((int32_t)num_neurons, seed, 0, num_inputs, Y0.data());
     if (rc) return die(e, rc, "sdnn_generate_inputs");
     if (write_data) {
-      ::mkdir(data.c_str(), 0755);
-      ::mkdir((data + "/tsv_weights").c_str(), 0755);
-      ::mkdir(weight_path.c_str(), 0755);
-      ::mkdir((data + "/MNIST").c_str(), 0755);
+      make_dirs(weight_path);
+      make_dirs(data + "/MNIST");
       if ((rc = sdnn_write_weights_tsv(e, weight_path.c_str()))) return die(e, rc, "write weights");
       if ((rc = sdnn_write_inputs_tsv(input_path.c_str(), Y0.data(), num_inputs, (int32_t)num_neurons)))
         return die(e, rc, "write inputs");

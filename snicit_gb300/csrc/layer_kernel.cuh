@@ -77,38 +77,52 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 __device__ __forceinline__ float clampf(float v, float hi) { return fminf(hi, fmaxf(0.f, v)); }
 
 // Accumulates the in-edges of group g from input chunk q into acc[T].
+// The slot indices (and values) of up to PF blocks are loaded into registers
+// before any of them is used, so a warp waits for one memory round trip per
+// PF blocks instead of one per block (the post-threshold launches have one
+// warp per group and nothing else to hide that latency).
 template <int T, int RSW, bool CONSTW>
 __device__ __forceinline__ void accumulate_group(float (&acc)[T], const LayerArgs& a,
                                                  const float* __restrict__ ys, int RS, int g,
                                                  int q, int lane) {
+  constexpr int PF = CONSTW ? 16 : 8;
   const int32_t b0 = __ldg(a.w.grp_blk + g * a.nq + q);
   const int32_t b1 = __ldg(a.w.grp_blk + g * a.nq + q + 1);
-  if (b0 >= b1) return;
   const uint2* __restrict__ ip = a.w.idx + (size_t)b0 * 32 + lane;
   const float4* __restrict__ vp = CONSTW ? nullptr : a.w.val + (size_t)b0 * 32 + lane;
   const float wc = a.w.wconst;
-  uint2 cur = __ldg(ip);
-  for (int b = 0; b < b1 - b0; ++b) {
-    uint2 nxt = cur;
-    if (b + 1 < b1 - b0) nxt = __ldg(ip + (size_t)(b + 1) * 32);
-    float wv[4];
-    if constexpr (!CONSTW) {
-      const float4 v0 = __ldg(vp + (size_t)b * 32);
-      wv[0] = v0.x; wv[1] = v0.y; wv[2] = v0.z; wv[3] = v0.w;
-    }
-    const uint32_t words[2] = {cur.x, cur.y};
+  const int nb = b1 - b0;
+  for (int bb = 0; bb < nb; bb += PF) {
+    uint2 iv[PF];
+    float4 vv[CONSTW ? 1 : PF];
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      const uint32_t j = (words[s >> 1] >> ((s & 1) * 16)) & 0xffffu;
-      const float* p = ys + j;
-      const float w = CONSTW ? wc : wv[s];
-#pragma unroll
-      for (int t = 0; t < T; ++t) {
-        const int off = (RSW > 0 ? RSW : RS) * t;
-        acc[t] = fmaf(w, p[off], acc[t]);
+    for (int k = 0; k < PF; ++k) {
+      if (bb + k < nb) {
+        iv[k] = __ldg(ip + (size_t)(bb + k) * 32);
+        if constexpr (!CONSTW) vv[k] = __ldg(vp + (size_t)(bb + k) * 32);
       }
     }
-    cur = nxt;
+#pragma unroll
+    for (int k = 0; k < PF; ++k) {
+      if (bb + k < nb) {
+        const uint32_t words[2] = {iv[k].x, iv[k].y};
+        float wv[4];
+        if constexpr (!CONSTW) {
+          wv[0] = vv[k].x; wv[1] = vv[k].y; wv[2] = vv[k].z; wv[3] = vv[k].w;
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const uint32_t j = (words[s >> 1] >> ((s & 1) * 16)) & 0xffffu;
+          const float* p = ys + j;
+          const float w = CONSTW ? wc : wv[s];
+#pragma unroll
+          for (int t = 0; t < T; ++t) {
+            const int off = (RSW > 0 ? RSW : RS) * t;
+            acc[t] = fmaf(w, p[off], acc[t]);
+          }
+        }
+      }
+    }
   }
 }
 
