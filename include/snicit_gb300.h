@@ -74,7 +74,7 @@ typedef struct sdnn_config {
   int32_t device;        /* CUDA device ordinal                                   */
   int32_t tile_rows;     /* rows per CTA in the layer kernel (0 = automatic)      */
   int32_t threads;       /* threads per CTA in the layer kernel (0 = automatic)   */
-  int32_t reserved[5];
+  int32_t reserved[5];   /* reserved[0] != 0 disables the binary first-layer path  */
 } sdnn_config;
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */

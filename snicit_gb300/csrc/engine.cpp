@@ -37,6 +37,7 @@ struct DevLayer {
   float4* val = nullptr;
   int32_t* grp = nullptr;
   float* bias = nullptr;
+  float* sums = nullptr;  // layer 0 with one common value: w added k times, k < 128
   bool constw = true;
   float wconst = 0.f;
   int64_t nnz = 0;
@@ -68,7 +69,7 @@ struct sdnn_engine {
   // kernel configuration
   int Q = 0, nq = 1, G = 0;
   LayerKernelKey key{};
-  int threads = 512, grid = 0, min_split = 1;
+  int threads = 512, grid = 0, grid_general = 0, min_split = 1;
   size_t smem = 0;
 
   // device weights
@@ -100,6 +101,9 @@ struct sdnn_engine {
   int32_t* d_ids = nullptr;
   int32_t* d_idcount = nullptr;
   float* d_in = nullptr;
+  int32_t* d_fallback = nullptr;  // layer-0 rows of non-binary tiles
+  int32_t* d_fbcount = nullptr;
+  int bits_grid = 0;
 
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
@@ -146,6 +150,7 @@ void free_weights(sdnn_engine* e) {
     dfree(d.val);
     dfree(d.grp);
     dfree(d.bias);
+    dfree(d.sums);
   }
   e->dl.clear();
 }
@@ -176,6 +181,8 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_ids);
   dfree(e->d_idcount);
   dfree(e->d_in);
+  dfree(e->d_fallback);
+  dfree(e->d_fbcount);
   e->cap = 0;
 }
 
@@ -211,7 +218,9 @@ int choose_kernel(sdnn_engine* e) {
     else if (rsw == 16416) Ts = {3, 2, 1};
     else Ts = {8, 4, 2, 1};
     for (int T : Ts) cands.push_back({T, rsw, 1, true});
-    if (rsw != 0)
+    // N = 1024 / 4096 store byte offsets (see slot_index_in_bytes), which only
+    // the instances with that compile-time row stride read
+    if (rsw == 16416)
       for (int T : {8, 4, 2, 1}) cands.push_back({T, 0, 1, true});
   } else {
     if (e->Q == 16384)
@@ -232,7 +241,8 @@ int choose_kernel(sdnn_engine* e) {
     e->key = k;
     e->smem = smem;
     e->threads = threads;
-    e->grid = e->num_sms * std::min(b1, b2);
+    e->grid = e->num_sms * b1;          // layers with one common weight value
+    e->grid_general = e->num_sms * b2;  // layers with per-edge values
     const int nwarps = threads / 32;
     e->min_split = k.kg > 1 ? (e->G + nwarps * k.kg - 1) / (nwarps * k.kg) : 1;
     return SDNN_OK;
@@ -282,6 +292,8 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_err, 16));
   T(A(&e->d_ids, (size_t)cap * 4));
   T(A(&e->d_idcount, 16));
+  T(A(&e->d_fallback, (size_t)cap * 4));
+  T(A(&e->d_fbcount, 16));
   if (rc != cudaSuccess) {
     free_buffers(e);
     cudaGetLastError();
@@ -320,7 +332,7 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
     h = &e->hw[l];
   }
   PackedLayer p;
-  if (!pack_layer(*h, e->N, e->Q, p)) {
+  if (!pack_layer(*h, e->N, e->Q, slot_index_in_bytes(e->Q) ? 4 : 1, p)) {
     err = "bad chunk size for packing";
     return SDNN_ERR_INVALID;
   }
@@ -346,6 +358,17 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
     T(cudaMemcpy(d.val, p.val.data(), p.val.size() * 4, cudaMemcpyHostToDevice));
   if (rc == cudaSuccess && d.bias)
     T(cudaMemcpy(d.bias, e->hbias[l].data(), (size_t)e->N * 4, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess && l == 0 && p.constw && p.max_depth < 128) {
+    // the float kernel adds w once per active edge: reproduce those sums
+    float sums[128];
+    float acc = 0.f;
+    for (int k = 0; k < 128; ++k) {
+      sums[k] = acc;
+      acc = acc + p.wconst;
+    }
+    T(cudaMalloc((void**)&d.sums, sizeof(sums)));
+    if (rc == cudaSuccess) T(cudaMemcpy(d.sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
+  }
   e->dl[l] = d;
   if (rc != cudaSuccess) {
     err = std::string("weight upload failed: ") + cudaGetErrorString(rc);
@@ -431,7 +454,7 @@ int layer_launch(sdnn_engine* e, int l, int epi, const float* in, float* out, co
   a.clampv = e->cfg.clamp;
   LayerKernelKey k = e->key;
   k.constw = d.constw;
-  CK(launch_layer(k, a, e->grid, e->threads, e->smem, e->stream));
+  CK(launch_layer(k, a, d.constw ? e->grid : e->grid_general, e->threads, e->smem, e->stream));
   e->launches++;
   return SDNN_OK;
 }
@@ -473,6 +496,33 @@ int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, b
       if ((rc = record(e, 2, capturing))) return rc;
     }
     const float* in = l == 0 ? d_in : e->d_y[(l - 1) & 1];
+    if (l == 0 && e->dl[0].sums && e->bits_grid > 0) {
+      // binary inputs: counting kernel; tiles with other values go to the float kernel
+      CK(cudaMemsetAsync(e->d_fbcount, 0, 16, s));
+      Layer0Args b{};
+      b.idx = e->dl[0].idx;
+      b.grp_blk = e->dl[0].grp;
+      b.bias_vec = e->dl[0].bias;
+      b.bias = e->cfg.bias;
+      b.clampv = e->cfg.clamp;
+      b.sums = e->dl[0].sums;
+      b.y_in = in;
+      b.y_out = e->d_y[0];
+      b.list_in = e->d_list[0];
+      b.count_in = e->d_counts;
+      b.list_out = e->d_list[1];
+      b.count_out = e->d_counts + 1;
+      b.fallback_list = e->d_fallback;
+      b.fallback_count = e->d_fbcount;
+      b.N = e->N;
+      b.G = e->G;
+      CK(launch_layer0_bits(b, e->bits_grid, 512, s));
+      e->launches++;
+      if ((rc = layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount,
+                             e->d_list[1], e->d_counts + 1)))
+        return rc;
+      continue;
+    }
     if ((rc = layer_launch(e, l, EPI_PLAIN, in, e->d_y[l & 1], e->d_list[l & 1], e->d_counts + l,
                            e->d_list[(l + 1) & 1], e->d_counts + l + 1)))
       return rc;
@@ -612,6 +662,9 @@ int prepare(sdnn_engine* e, int64_t rows) {
   }
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, true}, e->smem));
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
+  e->bits_grid = (e->nq == 1 && e->cfg.reserved[0] == 0 && layer0_bits_supported(e->N))
+                     ? layer0_bits_grid(e->N, e->num_sms, 512)
+                     : 0;
   return ensure_buffers(e, rows);
 }
 

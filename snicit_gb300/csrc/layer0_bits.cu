@@ -1,0 +1,193 @@
+// First-layer kernel for binary inputs (the SDGC input images are 0/1).
+//
+// When every input of a row is 0 or 1 and the layer has one common weight
+// value w, the pre-activation of output c is S(k) + b, where k is the number
+// of active in-edges of c and S(k) is w added k times in FP32 -- exactly what
+// the float gather (layer_kernel, which adds w * 1 or w * 0 slot by slot)
+// computes.  This kernel therefore counts instead of multiplying:
+//
+//  * a CTA owns 32 rows; warps read the rows coalesced and build, for every
+//    input j, one 32-bit word whose bit t is input j of row t (shared memory,
+//    N + 32 words, the last 32 zero for the padding slots);
+//  * lane i of a warp owns output 32g + i and walks the same bank-scheduled
+//    slots as layer_kernel, loading one word per slot (one wavefront per slot
+//    for all 32 rows) and adding it into bit-sliced counters with a
+//    Harley-Seal carry-save tree (15 full adders per 16 slots);
+//  * the epilogue extracts each row's count, looks up S(k) (a 128-entry table
+//    built on the host with the same FP32 additions), adds the bias, clamps,
+//    stores row t coalesced and ballots survivors into the next row list.
+//
+// A tile holding any value other than 0 or 1 is not computed here: its rows
+// go to a fallback list that the float kernel processes right after.
+#include <cstdint>
+#include "layer_kernel.cuh"
+
+namespace sdnn {
+
+__device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b, uint32_t c) {
+  const uint32_t u = a ^ b;
+  h = (a & b) | (u & c);
+  l = u ^ c;
+}
+
+template <int RSW>
+__global__ void __launch_bounds__(512, 1) layer0_bits_kernel(const Layer0Args a) {
+  extern __shared__ __align__(128) uint32_t bits[];  // RSW words
+  __shared__ float s_sum[128];
+  __shared__ int32_t s_rows[32];
+  __shared__ uint32_t s_mask;
+  __shared__ int32_t s_nonbin;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int N = a.N;
+  const int count = *a.count_in;
+  const int n_tiles = (count + 31) / 32;
+  if (tid < 128) s_sum[tid] = a.sums[tid];
+  for (int i = N + tid; i < RSW; i += blockDim.x) bits[i] = 0u;
+  __syncthreads();
+
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int row0 = tile * 32;
+    const int nrows = min(32, count - row0);
+    __syncthreads();
+    if (tid < 32) s_rows[tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
+    if (tid == 0) {
+      s_mask = 0;
+      s_nonbin = 0;
+    }
+    __syncthreads();
+    // transpose 32 rows into per-input bit words
+    bool nonbin = false;
+    for (int j0 = warp * 32; j0 < N; j0 += nwarps * 32) {
+      const int j = j0 + lane;
+      uint32_t word = 0;
+#pragma unroll 8
+      for (int t = 0; t < 32; ++t) {
+        if (t < nrows) {
+          const float v = __ldg(a.y_in + (size_t)s_rows[t] * N + j);
+          nonbin |= (v != 0.f) && (v != 1.f);
+          word |= (v != 0.f ? 1u : 0u) << t;
+        }
+      }
+      bits[j] = word;
+    }
+    if (__any_sync(0xffffffffu, nonbin) && lane == 0) s_nonbin = 1;
+    __syncthreads();
+    if (s_nonbin) {
+      if (tid < nrows) {
+        const int pos = atomicAdd(a.fallback_count, 1);
+        a.fallback_list[pos] = s_rows[tid];
+      }
+      continue;
+    }
+    uint32_t m = 0;
+    for (int g = warp; g < a.G; g += nwarps) {
+      const int32_t b0 = __ldg(a.grp_blk + g);
+      const int32_t b1 = __ldg(a.grp_blk + g + 1);
+      const uint2* __restrict__ ip = a.idx + (size_t)b0 * 32 + lane;
+      uint32_t ones = 0, twos = 0, fours = 0, eights = 0, sixteens = 0, thirtytwos = 0,
+               sixtyfours = 0;
+      for (int b = 0; b < b1 - b0; b += 4) {
+        uint32_t w[16];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          // blocks past the group's end read word 0 (in bounds) and add nothing
+          uint2 iv = make_uint2(0u, 0u);
+          if (b + k < b1 - b0) iv = __ldg(ip + (size_t)(b + k) * 32);
+#pragma unroll
+          for (int s = 0; s < 4; ++s) {
+            const uint32_t word = s < 2 ? iv.x : iv.y;
+            const uint32_t j = (word >> ((s & 1) * 16)) & 0xffffu;
+            const uint32_t* p = rsw_in_bytes(RSW)
+                                    ? reinterpret_cast<const uint32_t*>(
+                                          reinterpret_cast<const char*>(bits) + j)
+                                    : bits + j;
+            w[k * 4 + s] = (b + k < b1 - b0) ? *p : 0u;
+          }
+        }
+        uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, c16;
+        csa(twosA, ones, ones, w[0], w[1]);
+        csa(twosB, ones, ones, w[2], w[3]);
+        csa(foursA, twos, twos, twosA, twosB);
+        csa(twosA, ones, ones, w[4], w[5]);
+        csa(twosB, ones, ones, w[6], w[7]);
+        csa(foursB, twos, twos, twosA, twosB);
+        csa(eightsA, fours, fours, foursA, foursB);
+        csa(twosA, ones, ones, w[8], w[9]);
+        csa(twosB, ones, ones, w[10], w[11]);
+        csa(foursA, twos, twos, twosA, twosB);
+        csa(twosA, ones, ones, w[12], w[13]);
+        csa(twosB, ones, ones, w[14], w[15]);
+        csa(foursB, twos, twos, twosA, twosB);
+        csa(eightsB, fours, fours, foursA, foursB);
+        csa(c16, eights, eights, eightsA, eightsB);
+        uint32_t c = c16, t;
+        t = sixteens & c; sixteens ^= c; c = t;
+        t = thirtytwos & c; thirtytwos ^= c; c = t;
+        sixtyfours ^= c;
+      }
+      const int c_out = g * 32 + lane;
+      const float bc = a.bias_vec ? __ldg(a.bias_vec + c_out) : a.bias;
+      for (int t = 0; t < nrows; ++t) {
+        const uint32_t k = ((ones >> t) & 1u) | (((twos >> t) & 1u) << 1) |
+                           (((fours >> t) & 1u) << 2) | (((eights >> t) & 1u) << 3) |
+                           (((sixteens >> t) & 1u) << 4) | (((thirtytwos >> t) & 1u) << 5) |
+                           (((sixtyfours >> t) & 1u) << 6);
+        const float v = s_sum[k] + bc;
+        a.y_out[(size_t)s_rows[t] * N + c_out] = clampf(v, a.clampv);
+        if (__any_sync(0xffffffffu, v > 0.f)) m |= 1u << t;
+      }
+    }
+    if (lane == 0 && m) atomicOr(&s_mask, m);
+    __syncthreads();
+    if (tid == 0) {
+      const uint32_t mm = s_mask;
+      if (mm) {
+        const int base = atomicAdd(a.count_out, __popc(mm));
+        int i = 0;
+        for (int t = 0; t < 32; ++t)
+          if (mm & (1u << t)) a.list_out[base + i++] = s_rows[t];
+      }
+    }
+  }
+}
+
+template __global__ void layer0_bits_kernel<1056>(const Layer0Args);
+template __global__ void layer0_bits_kernel<4128>(const Layer0Args);
+template __global__ void layer0_bits_kernel<16416>(const Layer0Args);
+
+static const void* bits_fn(int rsw) {
+  switch (rsw) {
+    case 1056: return (const void*)&layer0_bits_kernel<1056>;
+    case 4128: return (const void*)&layer0_bits_kernel<4128>;
+    case 16416: return (const void*)&layer0_bits_kernel<16416>;
+    default: return nullptr;
+  }
+}
+
+bool layer0_bits_supported(int N) { return bits_fn(N + 32) != nullptr; }
+
+int layer0_bits_grid(int N, int num_sms, int threads) {
+  const void* fn = bits_fn(N + 32);
+  if (!fn) return 0;
+  const size_t smem = (size_t)(N + 32) * 4;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n * num_sms;
+}
+
+cudaError_t launch_layer0_bits(const Layer0Args& a, int grid, int threads, cudaStream_t s) {
+  const void* fn = bits_fn(a.N + 32);
+  if (!fn) return cudaErrorInvalidValue;
+  void* args[] = {const_cast<Layer0Args*>(&a)};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, (size_t)(a.N + 32) * 4, s);
+}
+
+}  // namespace sdnn

@@ -113,7 +113,10 @@ __device__ __forceinline__ void accumulate_group(float (&acc)[T], const LayerArg
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
           const uint32_t j = (words[s >> 1] >> ((s & 1) * 16)) & 0xffffu;
-          const float* p = ys + j;
+          // byte offset or float index, fixed by the packer for this row stride
+          const float* p = rsw_in_bytes(RSW)
+                               ? reinterpret_cast<const float*>(reinterpret_cast<const char*>(ys) + j)
+                               : ys + j;
           const float w = CONSTW ? wc : wv[s];
 #pragma unroll
           for (int t = 0; t < T; ++t) {

@@ -53,6 +53,12 @@ struct LayerArgs {
   float clampv;
 };
 
+// Chunk sizes whose packed slot indices are byte offsets into the shared row
+// (u16 holds (chunk + 32) * 4 only for chunks up to 16351 floats); the kernel
+// instances with row stride chunk + 32 of these chunk sizes read them as such.
+inline bool slot_index_in_bytes(int Q) { return Q == 1024 || Q == 4096; }
+__host__ __device__ constexpr bool rsw_in_bytes(int rsw) { return rsw == 1056 || rsw == 4128; }
+
 // Kernel instance selection.
 struct LayerKernelKey {
   int T;       // rows per tile
@@ -71,6 +77,27 @@ int layer_blocks_per_sm(const LayerKernelKey& key, int threads, size_t smem);
 bool layer_instance_exists(const LayerKernelKey& key);
 // Sets the max dynamic shared memory attribute of an instance.
 cudaError_t layer_prepare(const LayerKernelKey& key, size_t smem);
+
+// First layer over binary inputs (layer0_bits.cu).
+struct Layer0Args {
+  const uint2* idx;          // packed slots of layer 0 (same layout as LayerDev)
+  const int32_t* grp_blk;    // [G + 1]
+  const float* bias_vec;     // [N] or nullptr
+  float bias, clampv;
+  const float* sums;         // [128]: w added k times in FP32, k = 0..127
+  const float* y_in;
+  float* y_out;
+  const int32_t* list_in;
+  const int32_t* count_in;
+  int32_t* list_out;
+  int32_t* count_out;
+  int32_t* fallback_list;    // rows of tiles with non-binary inputs
+  int32_t* fallback_count;
+  int32_t N, G;
+};
+bool layer0_bits_supported(int N);
+int layer0_bits_grid(int N, int num_sms, int threads);
+cudaError_t launch_layer0_bits(const Layer0Args& a, int grid, int threads, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);

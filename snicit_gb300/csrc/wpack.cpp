@@ -66,8 +66,9 @@ struct SlotSet {
 
 }  // namespace
 
-bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out) {
-  if (Q <= 0 || Q % 32 != 0 || N % Q != 0 || Q + 32 > 65536) return false;
+bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedLayer& out) {
+  if (Q <= 0 || Q % 32 != 0 || N % Q != 0 || (scale != 1 && scale != 4)) return false;
+  if ((int64_t)(Q + 31) * scale > 65535) return false;
   const int32_t G = N / 32, nq = N / Q;
   // CSC: in-edges of every output, inputs ascending.
   std::vector<int32_t> indeg(N + 1, 0);
@@ -165,12 +166,12 @@ bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out) {
           const int32_t k = slot_lane_edge[(size_t)s * 32 + l];
           const size_t at = base + (size_t)b * 128 + (size_t)l * 4 + si;
           if (k >= 0) {
-            out.idx[at] = (uint16_t)edges[k].jl;
+            out.idx[at] = (uint16_t)(edges[k].jl * scale);
             if (!out.constw) out.val[at] = edges[k].w;
           } else {
             const int fb = __builtin_ctz(free_banks);
             free_banks &= free_banks - 1;
-            out.idx[at] = (uint16_t)(Q + fb);  // zero column in the bank left free
+            out.idx[at] = (uint16_t)((Q + fb) * scale);  // zero column in the bank left free
             if (!out.constw) out.val[at] = 0.f;
           }
         }

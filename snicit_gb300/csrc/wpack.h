@@ -36,8 +36,9 @@ struct PackedLayer {
   int64_t slots = 0;             // total slots (sum of depths)
 };
 
-// Packs one layer for chunk size Q (N % Q == 0, Q % 32 == 0, Q + 32 <= 65536);
-// returns false when Q violates that.
-bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, PackedLayer& out);
+// Packs one layer for chunk size Q (N % Q == 0, Q % 32 == 0); slot indices are
+// stored as (chunk-local index) * scale, scale 4 = byte offsets, 1 = floats;
+// returns false when (Q + 32) * scale does not fit 16 bits or Q is invalid.
+bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedLayer& out);
 
 }  // namespace sdnn

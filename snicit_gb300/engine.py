@@ -21,7 +21,7 @@ class Engine:
 
     def __init__(self, num_neurons=1024, num_layers=120, mode="SNICIT", threshold=30,
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
-                 device=0, tile_rows=0, threads=0):
+                 device=0, tile_rows=0, threads=0, binary_first_layer=True):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -37,6 +37,7 @@ class Engine:
         cfg.device = int(device)
         cfg.tile_rows = int(tile_rows)
         cfg.threads = int(threads)
+        cfg.reserved[0] = 0 if binary_first_layer else 1
         self.cfg = cfg
         self.N = cfg.num_neurons
         self.L = cfg.num_layers

@@ -258,3 +258,23 @@ def test_autotune_keeps_categories():
     _, alive, _ = orc.infer(_layers(N, L, seed), N, -0.3, Y0, precision=64, want_y=False)
     assert surv == {int(alive.sum())}
     assert np.array_equal(ids, np.flatnonzero(alive))
+
+
+@pytest.mark.parametrize("N,L,B", [(1024, 8, 700), (4096, 5, 300), (16384, 3, 70)])
+def test_binary_first_layer_is_bitwise_equal(N, L, B):
+    """The counting first-layer kernel gives the float kernel's bits exactly;
+    tiles with a non-binary value fall back to the float kernel."""
+    seed = 5 + N
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    Y0[40, 3] = 0.5  # one non-binary value: its 32-row tile takes the fallback
+    out = {}
+    for fast in (True, False):
+        with sg.Engine(N, L, mode="SNIG", batch=B, bias=sg.load().sdnn_reference_bias(N),
+                       binary_first_layer=fast) as eng:
+            eng.generate_weights(seed)
+            flags, ids = eng.infer(Y0)
+            out[fast] = (flags, ids, eng.activations(B))
+    assert np.array_equal(out[True][1], out[False][1])
+    assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
+    Yref, alive, Y32 = _ref(_layers(N, L, seed), N, sg.load().sdnn_reference_bias(N), Y0)
+    _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"bits N={N}", Y32=Y32)
