@@ -74,8 +74,14 @@ typedef struct sdnn_config {
   int32_t device;        /* CUDA device ordinal                                   */
   int32_t tile_rows;     /* rows per CTA in the layer kernel (0 = automatic)      */
   int32_t threads;       /* threads per CTA in the layer kernel (0 = automatic)   */
-  int32_t reserved[5];   /* reserved[0] != 0 disables the binary first-layer path  */
+  int32_t flags;         /* SDNN_FLAG_* bits (0 = all optimisations on)            */
+  int32_t reserved[4];
 } sdnn_config;
+
+/* sdnn_config.flags: switch off layout optimisations (results are identical
+ * either way; used to compare the paths). */
+#define SDNN_FLAG_NO_BINARY_FIRST_LAYER 1  /* float kernel for layer 0 even for 0/1 inputs */
+#define SDNN_FLAG_NO_PLACEMENT 2           /* keep neuron order; no degree/bank placement   */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -175,6 +181,12 @@ int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows);
 
 /* Statistics of the last inference. */
 int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
+
+/* Rows processed by every layer of the last inference (plain rows for layers
+ * below the threshold, centroid + non-empty residue rows above it); out has
+ * room for num_layers entries.  (The reference prints these counts only as
+ * debugging output, src/SDGC/XY/XY.hpp:481.) */
+int sdnn_get_layer_rows(const sdnn_engine* e, int64_t* out, int32_t num_layers);
 
 /* Chooses threshold, centroid count and tile shape by timing the candidates
  * on the given sample rows (host buffer) and appends one JSON line per tried

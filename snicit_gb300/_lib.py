@@ -10,6 +10,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libsnicit_gb300.so")
 
 MODES = {"BF": 0, "SNIG": 1, "XY": 2, "SNICIT": 3}
+FLAG_NO_BINARY_FIRST_LAYER = 1
+FLAG_NO_PLACEMENT = 2
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",
@@ -31,7 +33,7 @@ class Config(ctypes.Structure):
         ("bias", ctypes.c_float), ("clamp", ctypes.c_float), ("num_centroids", ctypes.c_int32),
         ("autotune", ctypes.c_int32), ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
         ("tile_rows", ctypes.c_int32), ("threads", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("flags", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
     ]
 
 
@@ -68,6 +70,7 @@ SIGNATURES = [
     ("sdnn_read_inputs_tsv", ctypes.c_int, [ctypes.c_char_p, I32, I64, I64, P]),
     ("sdnn_read_activations", ctypes.c_int, [P, P, I64]),
     ("sdnn_get_stats", ctypes.c_int, [P, P]),
+    ("sdnn_get_layer_rows", ctypes.c_int, [P, P, I32]),
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_generate_inputs", ctypes.c_int, [I32, U64, I64, I64, P]),
     ("sdnn_generate_layer_coo", ctypes.c_int, [I32, U64, I32, I32, F32, P, P, P]),

@@ -342,35 +342,36 @@ void launch_recover(const float* y, const int32_t* live, const int32_t* live_cou
                                      flags);
 }
 
-// Final activations per row: state 0 -> zeros (dead), 1 -> copy of the final
-// buffer (plain modes), 2 -> SNICIT recovery (centroid, or centroid + residue).
+// Final activations per row, in neuron order (out[r][c] reads position perm[c]):
+// state 0 -> zeros (dead), 1 -> copy of the final buffer (plain modes),
+// 2 -> SNICIT recovery (centroid, or centroid + residue).
 __global__ void materialize_kernel(const float* __restrict__ y, const int32_t* state,
                                    const int32_t* cslot, const int32_t* clist,
                                    const int32_t* is_centroid, const int32_t* res_flag,
-                                   int32_t N, int32_t rows, float* out) {
+                                   const int32_t* perm, int32_t N, int32_t rows, float* out) {
   for (int r = blockIdx.x; r < rows; r += gridDim.x) {
     float* o = out + (size_t)r * N;
     const int st = state[r];
     const float* yr = y + (size_t)r * N;
     if (st == 0) {
       for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = 0.f;
-    } else if (st == 1 || is_centroid[r]) {
-      for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = yr[j];
-    } else {
-      const float* yc = y + (size_t)clist[cslot[r]] * N;
-      if (res_flag[r]) {
-        for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = yr[j] + yc[j];
-      } else {
-        for (int j = threadIdx.x; j < N; j += blockDim.x) o[j] = yc[j];
-      }
+      continue;
+    }
+    const bool plain = st == 1 || is_centroid[r];
+    const float* yc = plain ? yr : y + (size_t)clist[cslot[r]] * N;
+    const bool has_res = !plain && res_flag[r];
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const int p = perm ? perm[j] : j;
+      o[j] = plain ? yr[p] : (has_res ? yr[p] + yc[p] : yc[p]);
     }
   }
 }
+
 void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
                         const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
-                        int32_t N, float* out, int32_t rows, cudaStream_t s) {
+                        const int32_t* perm, int32_t N, float* out, int32_t rows, cudaStream_t s) {
   materialize_kernel<<<grid_for(rows, 1, 8192), 256, 0, s>>>(y, state, cslot, clist, is_centroid,
-                                                             res_flag, N, rows, out);
+                                                             res_flag, perm, N, rows, out);
 }
 
 }  // namespace sdnn

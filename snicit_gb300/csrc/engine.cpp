@@ -75,6 +75,9 @@ struct sdnn_engine {
   // device weights
   std::vector<DevLayer> dl;
   int64_t total_nnz = 0;
+  // neuron placement: positions of the outputs of every layer (empty = identity)
+  std::vector<std::vector<int32_t>> pos;
+  int32_t* d_perm_final = nullptr;  // position of neuron c after the last layer
 
   // device buffers
   int64_t cap = 0;
@@ -145,6 +148,7 @@ void dfree(T*& p) {
 }
 
 void free_weights(sdnn_engine* e) {
+  dfree(e->d_perm_final);
   for (auto& d : e->dl) {
     dfree(d.idx);
     dfree(d.val);
@@ -306,33 +310,36 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   return SDNN_OK;
 }
 
-// Builds one layer (generated or given), packs it and uploads it.
+// The host CSR of layer l: regenerated for synthetic weights, else stored.
+const HostLayer* host_layer(sdnn_engine* e, int l, HostLayer& tmp) {
+  if (!e->gen.on) return e->hw[l].present ? &e->hw[l] : nullptr;
+  const int N = e->N, k = e->gen.nnz;
+  tmp.row_off.resize(N + 1);
+  tmp.cols.resize((size_t)N * k);
+  tmp.vals.assign((size_t)N * k, e->gen.value);
+  for (int j = 0; j < N; ++j) {
+    tmp.row_off[j] = j * k;
+    int32_t* c = tmp.cols.data() + (size_t)j * k;
+    gen_row_cols(e->gen.seed, l, j, N, k, c);
+    std::sort(c, c + k);
+  }
+  tmp.row_off[N] = N * k;
+  tmp.present = true;
+  return &tmp;
+}
+
+// Packs layer l with the chosen neuron placement and uploads it.
 int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   HostLayer tmp;
-  const HostLayer* h = nullptr;
-  if (e->gen.on) {
-    const int N = e->N, k = e->gen.nnz;
-    tmp.row_off.resize(N + 1);
-    tmp.cols.resize((size_t)N * k);
-    tmp.vals.assign((size_t)N * k, e->gen.value);
-    for (int j = 0; j < N; ++j) {
-      tmp.row_off[j] = j * k;
-      int32_t* c = tmp.cols.data() + (size_t)j * k;
-      gen_row_cols(e->gen.seed, l, j, N, k, c);
-      std::sort(c, c + k);
-    }
-    tmp.row_off[N] = N * k;
-    tmp.present = true;
-    h = &tmp;
-  } else {
-    if (!e->hw[l].present) {
-      err = "layer " + std::to_string(l) + " has no weights";
-      return SDNN_ERR_STATE;
-    }
-    h = &e->hw[l];
+  const HostLayer* h = host_layer(e, l, tmp);
+  if (!h) {
+    err = "layer " + std::to_string(l) + " has no weights";
+    return SDNN_ERR_STATE;
   }
+  const int32_t* in_pos = (l > 0 && !e->pos.empty()) ? e->pos[l - 1].data() : nullptr;
+  const int32_t* out_pos = e->pos.empty() ? nullptr : e->pos[l].data();
   PackedLayer p;
-  if (!pack_layer(*h, e->N, e->Q, slot_index_in_bytes(e->Q) ? 4 : 1, p)) {
+  if (!pack_layer_placed(*h, e->N, e->Q, slot_index_in_bytes(e->Q) ? 4 : 1, in_pos, out_pos, p)) {
     err = "bad chunk size for packing";
     return SDNN_ERR_INVALID;
   }
@@ -349,15 +356,19 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   T(cudaMalloc((void**)&d.idx, std::max<size_t>(p.idx.size() * 2, 16)));
   T(cudaMalloc((void**)&d.grp, p.grp_blk.size() * 4));
   if (!p.constw) T(cudaMalloc((void**)&d.val, std::max<size_t>(p.val.size() * 4, 16)));
-  if (l < (int)e->hbias.size() && !e->hbias[l].empty())
-    T(cudaMalloc((void**)&d.bias, (size_t)e->N * 4));
+  const bool has_bias = l < (int)e->hbias.size() && !e->hbias[l].empty();
+  if (has_bias) T(cudaMalloc((void**)&d.bias, (size_t)e->N * 4));
   if (rc == cudaSuccess && !p.idx.empty())
     T(cudaMemcpy(d.idx, p.idx.data(), p.idx.size() * 2, cudaMemcpyHostToDevice));
   if (rc == cudaSuccess) T(cudaMemcpy(d.grp, p.grp_blk.data(), p.grp_blk.size() * 4, cudaMemcpyHostToDevice));
   if (rc == cudaSuccess && d.val && !p.val.empty())
     T(cudaMemcpy(d.val, p.val.data(), p.val.size() * 4, cudaMemcpyHostToDevice));
-  if (rc == cudaSuccess && d.bias)
-    T(cudaMemcpy(d.bias, e->hbias[l].data(), (size_t)e->N * 4, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess && has_bias) {
+    // per-neuron bias follows its neuron to its position
+    std::vector<float> b(e->N);
+    for (int c = 0; c < e->N; ++c) b[out_pos ? out_pos[c] : c] = e->hbias[l][c];
+    T(cudaMemcpy(d.bias, b.data(), (size_t)e->N * 4, cudaMemcpyHostToDevice));
+  }
   if (rc == cudaSuccess && l == 0 && p.constw && p.max_depth < 128) {
     // the float kernel adds w once per active edge: reproduce those sums
     float sums[128];
@@ -377,17 +388,9 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   return SDNN_OK;
 }
 
-int finalize_weights(sdnn_engine* e) {
-  if (!e->weights_dirty) return SDNN_OK;
-  if (!e->gen.on) {
-    if ((int)e->hw.size() != e->L) return fail(e, SDNN_ERR_STATE, "weights not loaded");
-    for (int l = 0; l < e->L; ++l)
-      if (!e->hw[l].present)
-        return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
-  }
-  drop_graph(e);
-  free_weights(e);
-  e->dl.assign(e->L, DevLayer{});
+// Runs fn(l, err) for every layer on a small thread pool; first error wins.
+template <typename Fn>
+int for_layers(sdnn_engine* e, Fn fn) {
   int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   nthreads = std::min(nthreads, e->L);
   std::atomic<int> next{0};
@@ -398,7 +401,7 @@ int finalize_weights(sdnn_engine* e) {
     for (;;) {
       const int l = next.fetch_add(1);
       if (l >= e->L || status.load() != SDNN_OK) break;
-      const int rc = pack_upload_layer(e, l, errs[id]);
+      const int rc = fn(l, errs[id]);
       if (rc != SDNN_OK) {
         int expected = SDNN_OK;
         status.compare_exchange_strong(expected, rc);
@@ -411,10 +414,57 @@ int finalize_weights(sdnn_engine* e) {
   for (auto& t : pool) t.join();
   if (status.load() != SDNN_OK) {
     std::string msg;
-    for (auto& s : errs)
-      if (!s.empty()) msg = s;
+    for (auto& m : errs)
+      if (!m.empty()) msg = m;
+    e->err = msg;
+  }
+  return status.load();
+}
+
+// Packs every layer.  With whole-row layouts (one chunk) the neurons of each
+// layer are first placed: outputs grouped by in-degree (so the 32 lanes of a
+// group have nearly equal slot lists) and given lanes that balance the bank
+// loads of the next layer, which shortens the bank-scheduled slot lists.
+int finalize_weights(sdnn_engine* e) {
+  if (!e->weights_dirty) return SDNN_OK;
+  if (!e->gen.on) {
+    if ((int)e->hw.size() != e->L) return fail(e, SDNN_ERR_STATE, "weights not loaded");
+    for (int l = 0; l < e->L; ++l)
+      if (!e->hw[l].present)
+        return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
+  }
+  drop_graph(e);
+  free_weights(e);
+  e->dl.assign(e->L, DevLayer{});
+  e->pos.clear();
+  const bool place = e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
+  int rc;
+  if (place) {
+    std::vector<std::vector<int32_t>> order(e->L);
+    rc = for_layers(e, [&](int l, std::string&) {
+      HostLayer tmp;
+      order[l] = degree_order(*host_layer(e, l, tmp), e->N);
+      return SDNN_OK;
+    });
+    if (rc) return rc;
+    e->pos.resize(e->L);
+    rc = for_layers(e, [&](int l, std::string&) {
+      HostLayer tmp;
+      const HostLayer* next = l + 1 < e->L ? host_layer(e, l + 1, tmp) : nullptr;
+      e->pos[l] = place_outputs(order[l], next, next ? &order[l + 1] : nullptr, e->N);
+      return SDNN_OK;
+    });
+    if (rc) return rc;
+  }
+  rc = for_layers(e, [&](int l, std::string& err) { return pack_upload_layer(e, l, err); });
+  if (rc) {
     free_weights(e);
-    return fail(e, status.load(), msg);
+    return rc;
+  }
+  if (!e->pos.empty()) {
+    CK(cudaMalloc((void**)&e->d_perm_final, (size_t)e->N * 4));
+    CK(cudaMemcpy(e->d_perm_final, e->pos[e->L - 1].data(), (size_t)e->N * 4,
+                  cudaMemcpyHostToDevice));
   }
   e->total_nnz = 0;
   for (auto& d : e->dl) e->total_nnz += d.nnz;
@@ -662,7 +712,8 @@ int prepare(sdnn_engine* e, int64_t rows) {
   }
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, true}, e->smem));
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
-  e->bits_grid = (e->nq == 1 && e->cfg.reserved[0] == 0 && layer0_bits_supported(e->N))
+  e->bits_grid = (e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
+                  layer0_bits_supported(e->N))
                      ? layer0_bits_grid(e->N, e->num_sms, 512)
                      : 0;
   return ensure_buffers(e, rows);
@@ -955,7 +1006,7 @@ int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows) {
   const int L = e->L;
   float* scratch = e->d_y[L & 1];
   launch_materialize(e->d_y[(L - 1) & 1], e->d_state, e->d_cslot, e->d_clist, e->d_iscent,
-                     e->d_resflag, e->N, scratch, (int32_t)rows, e->stream);
+                     e->d_resflag, e->d_perm_final, e->N, scratch, (int32_t)rows, e->stream);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, scratch, (size_t)rows * e->N * 4, cudaMemcpyDeviceToHost, e->stream));
   CK(cudaStreamSynchronize(e->stream));
@@ -975,27 +1026,31 @@ int sdnn_get_stats(const sdnn_engine* ce, sdnn_stats* out) {
   return SDNN_OK;
 }
 
+int sdnn_get_layer_rows(const sdnn_engine* ce, int64_t* out, int32_t num_layers) {
+  if (!ce || !out || num_layers < ce->L) return SDNN_ERR_INVALID;
+  auto* e = const_cast<sdnn_engine*>(ce);
+  if (!e->have_run) return fail(e, SDNN_ERR_STATE, "no inference has run");
+  CK(cudaSetDevice(e->dev));
+  CK(cudaStreamSynchronize(e->stream));
+  const int L = e->L, T = e->last_T;
+  std::vector<int32_t> counts(L + 4), rcounts(L + 4);
+  int32_t ccount = 0;
+  CK(cudaMemcpy(counts.data(), e->d_counts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
+  for (int l = 0; l < T; ++l) out[l] = counts[l];
+  if (T < L) {
+    CK(cudaMemcpy(rcounts.data(), e->d_rcounts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ccount, e->d_ccount, 4, cudaMemcpyDeviceToHost));
+    for (int l = T; l < L; ++l) out[l] = (int64_t)ccount + rcounts[l - T];
+  }
+  return SDNN_OK;
+}
+
 int sdnn_write_weights_tsv(sdnn_engine* e, const char* dir) {
   if (!e || !dir) return SDNN_ERR_INVALID;
   for (int l = 0; l < e->L; ++l) {
     HostLayer tmp;
-    const HostLayer* h = &e->hw[l];
-    if (e->gen.on) {
-      const int N = e->N, k = e->gen.nnz;
-      tmp.row_off.resize(N + 1);
-      tmp.cols.resize((size_t)N * k);
-      tmp.vals.assign((size_t)N * k, e->gen.value);
-      for (int j = 0; j < N; ++j) {
-        tmp.row_off[j] = j * k;
-        int32_t* c = tmp.cols.data() + (size_t)j * k;
-        gen_row_cols(e->gen.seed, l, j, N, k, c);
-        std::sort(c, c + k);
-      }
-      tmp.row_off[N] = N * k;
-      h = &tmp;
-    } else if (!h->present) {
-      return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
-    }
+    const HostLayer* h = host_layer(e, l, tmp);
+    if (!h) return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
     const std::string p =
         std::string(dir) + "/n" + std::to_string(e->N) + "-l" + std::to_string(l + 1) + ".tsv";
     int rc = write_weight_tsv(p, *h, e->N);

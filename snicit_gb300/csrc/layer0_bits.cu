@@ -6,9 +6,10 @@
 // the float gather (layer_kernel, which adds w * 1 or w * 0 slot by slot)
 // computes.  This kernel therefore counts instead of multiplying:
 //
-//  * a CTA owns 32 rows; warps read the rows coalesced and build, for every
-//    input j, one 32-bit word whose bit t is input j of row t (shared memory,
-//    N + 32 words, the last 32 zero for the padding slots);
+//  * a CTA owns 32 rows; warps read the rows coalesced (16-byte loads, 8 rows
+//    in flight per lane) and build, for every input j, one 32-bit word whose
+//    bit t is input j of row t (shared memory, N + 32 words, the last 32 zero
+//    for the padding slots; N is a multiple of 128);
 //  * lane i of a warp owns output 32g + i and walks the same bank-scheduled
 //    slots as layer_kernel, loading one word per slot (one wavefront per slot
 //    for all 32 rows) and adding it into bit-sliced counters with a
@@ -56,20 +57,33 @@ __global__ void __launch_bounds__(512, 1) layer0_bits_kernel(const Layer0Args a)
       s_nonbin = 0;
     }
     __syncthreads();
-    // transpose 32 rows into per-input bit words
+    // transpose 32 rows into per-input bit words: lane takes 4 consecutive
+    // inputs (one 16-byte load per row), 8 rows of loads in flight at a time
     bool nonbin = false;
-    for (int j0 = warp * 32; j0 < N; j0 += nwarps * 32) {
-      const int j = j0 + lane;
-      uint32_t word = 0;
-#pragma unroll 8
-      for (int t = 0; t < 32; ++t) {
-        if (t < nrows) {
-          const float v = __ldg(a.y_in + (size_t)s_rows[t] * N + j);
-          nonbin |= (v != 0.f) && (v != 1.f);
-          word |= (v != 0.f ? 1u : 0u) << t;
+    for (int j0 = warp * 128; j0 < N; j0 += nwarps * 128) {
+      const int j = j0 + lane * 4;
+      uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+      for (int t0 = 0; t0 < nrows; t0 += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (t0 + u < nrows)
+            v[u] = __ldg(reinterpret_cast<const float4*>(a.y_in + (size_t)s_rows[t0 + u] * N + j));
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (t0 + u < nrows) {
+            const float x[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) nonbin |= (x[q] != 0.f) && (x[q] != 1.f);
+            const uint32_t bit = 1u << (t0 + u);
+            w0 |= x[0] != 0.f ? bit : 0u;
+            w1 |= x[1] != 0.f ? bit : 0u;
+            w2 |= x[2] != 0.f ? bit : 0u;
+            w3 |= x[3] != 0.f ? bit : 0u;
+          }
         }
       }
-      bits[j] = word;
+      *reinterpret_cast<uint4*>(bits + j) = make_uint4(w0, w1, w2, w3);
     }
     if (__any_sync(0xffffffffu, nonbin) && lane == 0) s_nonbin = 1;
     __syncthreads();

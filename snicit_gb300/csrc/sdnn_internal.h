@@ -137,8 +137,9 @@ void launch_recover(const float* y, const int32_t* live, const int32_t* live_cou
                     const int32_t* res_flag, int32_t N, int32_t* flags, cudaStream_t s);
 // Final activations of every row into out[rows][N]: state 0 = dead (zeros),
 // 1 = plain final row, 2 = SNICIT live row (centroid, or centroid + residue).
+// perm[c] = position of neuron c in the final buffer (nullptr = identity).
 void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
                         const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
-                        int32_t N, float* out, int32_t rows, cudaStream_t s);
+                        const int32_t* perm, int32_t N, float* out, int32_t rows, cudaStream_t s);
 
 }  // namespace sdnn

@@ -5,12 +5,15 @@
 // group) and shared-memory banks (input index mod 32).  A proper edge
 // colouring of that graph is a slot schedule in which every slot touches 32
 // distinct banks (and each lane at most once), so the gather in the layer
-// kernel never has a bank conflict.  König's theorem bounds the optimum by the
-// maximum degree; greedy first-fit colouring (each edge takes the lowest slot
-// free at its lane and its bank) stays within a few slots of it.
+// kernel never has a bank conflict.  By König's theorem the maximum degree
+// (largest lane in-degree or bank load) colours suffice; EdgeColoring reaches
+// that bound with alternating-path (Kempe chain) recolouring.
 #include "wpack.h"
 
 #include <algorithm>
+#include <array>
+#include <climits>
+#include <cstdint>
 #include <numeric>
 
 namespace sdnn {
@@ -53,18 +56,164 @@ bool coo_to_host_layer(int32_t N, const int32_t* rows, const int32_t* cols, cons
 
 namespace {
 
-// Bitset of slot indices, grown on demand.
-struct SlotSet {
-  std::vector<uint64_t> w;
-  void set(int s) {
-    if ((size_t)(s >> 6) >= w.size()) w.resize((s >> 6) + 1, 0);
-    w[s >> 6] |= 1ull << (s & 63);
+// Proper edge colouring of a bipartite multigraph with exactly Delta colours
+// (Delta = maximum vertex degree), by Kempe-chain recolouring: an edge (u, v)
+// takes a colour a free at u; if a is taken at v, the a/b alternating path
+// from v (b free at v) is flipped first, which frees a at v and, the graph
+// being bipartite, cannot reach u.  Vertices 0..31 are lanes, 32..63 banks.
+class EdgeColoring {
+ public:
+  explicit EdgeColoring(int max_colors) : C_(max_colors), at_(64 * (size_t)max_colors, -1) {}
+  void reset(int max_colors) {
+    C_ = max_colors;
+    at_.assign(64 * (size_t)C_, -1);
+    colour_.clear();
+    ends_.clear();
   }
-  uint64_t word(size_t i) const { return i < w.size() ? w[i] : 0; }
-  void clear() { std::fill(w.begin(), w.end(), 0); }
+  // returns the colour of the new edge
+  int add(int lane, int bank) {
+    const int u = lane, v = 32 + bank;
+    const int e = (int)colour_.size();
+    colour_.push_back(-1);
+    ends_.push_back({u, v});
+    const int a = first_free(u), b = first_free(v);
+    int c;
+    if (is_free(v, a)) {
+      c = a;
+    } else if (is_free(u, b)) {
+      c = b;
+    } else {
+      flip(v, a, b);
+      c = a;
+    }
+    set(e, c);
+    return c;
+  }
+  int colour(int e) const { return colour_[e]; }
+
+ private:
+  int& slot(int vertex, int c) { return at_[(size_t)vertex * C_ + c]; }
+  bool is_free(int vertex, int c) { return slot(vertex, c) < 0; }
+  int first_free(int vertex) {
+    for (int c = 0; c < C_; ++c)
+      if (slot(vertex, c) < 0) return c;
+    return -1;  // cannot happen: degree <= C_
+  }
+  void set(int e, int c) {
+    colour_[e] = c;
+    slot(ends_[e][0], c) = e;
+    slot(ends_[e][1], c) = e;
+  }
+  // swaps colours a and b on the alternating path that starts at w with colour a
+  void flip(int w, int a, int b) {
+    path_.clear();
+    int col = a;
+    for (;;) {
+      const int e = slot(w, col);
+      if (e < 0) break;
+      path_.push_back(e);
+      w = ends_[e][0] == w ? ends_[e][1] : ends_[e][0];
+      col = col == a ? b : a;
+    }
+    for (int e : path_) {
+      slot(ends_[e][0], colour_[e]) = -1;
+      slot(ends_[e][1], colour_[e]) = -1;
+    }
+    for (int e : path_) set(e, colour_[e] == a ? b : a);
+  }
+  int C_;
+  std::vector<int> at_;  // [vertex][colour] -> edge or -1
+  std::vector<int> colour_;
+  std::vector<std::array<int, 2>> ends_;
+  std::vector<int> path_;
 };
 
 }  // namespace
+
+bool pack_layer_placed(const HostLayer& hin, int32_t N, int32_t Q, int32_t scale,
+                       const int32_t* in_pos, const int32_t* out_pos, PackedLayer& out) {
+  if (!in_pos && !out_pos) return pack_layer(hin, N, Q, scale, out);
+  // relabel rows (inputs) and columns (outputs), keep per-row column order sorted
+  HostLayer h;
+  h.row_off.assign(N + 1, 0);
+  for (int32_t j = 0; j < N; ++j) {
+    const int32_t pj = in_pos ? in_pos[j] : j;
+    h.row_off[pj + 1] = hin.row_off[j + 1] - hin.row_off[j];
+  }
+  for (int32_t j = 0; j < N; ++j) h.row_off[j + 1] += h.row_off[j];
+  h.cols.resize(hin.cols.size());
+  h.vals.resize(hin.vals.size());
+  std::vector<std::pair<int32_t, float>> tmp;
+  for (int32_t j = 0; j < N; ++j) {
+    const int32_t pj = in_pos ? in_pos[j] : j;
+    tmp.clear();
+    for (int32_t k = hin.row_off[j]; k < hin.row_off[j + 1]; ++k)
+      tmp.push_back({out_pos ? out_pos[hin.cols[k]] : hin.cols[k], hin.vals[k]});
+    std::sort(tmp.begin(), tmp.end(),
+              [](const std::pair<int32_t, float>& a, const std::pair<int32_t, float>& b) {
+                return a.first < b.first;
+              });
+    for (size_t k = 0; k < tmp.size(); ++k) {
+      h.cols[h.row_off[pj] + k] = tmp[k].first;
+      h.vals[h.row_off[pj] + k] = tmp[k].second;
+    }
+  }
+  h.present = true;
+  return pack_layer(h, N, Q, scale, out);
+}
+
+std::vector<int32_t> degree_order(const HostLayer& h, int32_t N) {
+  std::vector<int32_t> deg(N, 0), order(N);
+  for (int32_t c : h.cols) deg[c]++;
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+  return order;
+}
+
+std::vector<int32_t> place_outputs(const std::vector<int32_t>& order, const HostLayer* next,
+                                   const std::vector<int32_t>* next_order, int32_t N) {
+  std::vector<int32_t> pos(N);
+  const int32_t G = N / 32;
+  if (!next || !next_order) {
+    for (int32_t i = 0; i < N; ++i) pos[order[i]] = i;
+    return pos;
+  }
+  std::vector<int32_t> gnext(N);
+  for (int32_t i = 0; i < N; ++i) gnext[(*next_order)[i]] = i / 32;
+  std::vector<int32_t> load((size_t)G * 32, 0);
+  std::vector<int32_t> nodes(32);
+  for (int32_t g = 0; g < G; ++g) {
+    for (int i = 0; i < 32; ++i) nodes[i] = order[32 * g + i];
+    // neurons with more out-edges first; each takes the free bank that adds the
+    // least squared load to the next-layer groups it feeds
+    std::stable_sort(nodes.begin(), nodes.end(), [&](int32_t a, int32_t b) {
+      return next->row_off[a + 1] - next->row_off[a] > next->row_off[b + 1] - next->row_off[b];
+    });
+    uint32_t used = 0;
+    for (int32_t n : nodes) {
+      int best = -1;
+      int64_t best_cost = INT64_MAX;
+      for (int b = 0; b < 32; ++b) {
+        if (used & (1u << b)) continue;
+        int64_t cost = 0;
+        for (int32_t k = next->row_off[n]; k < next->row_off[n + 1]; ++k) {
+          const int64_t ld = load[(size_t)gnext[next->cols[k]] * 32 + b];
+          cost += 2 * ld + 1;
+        }
+        if (cost < best_cost) {
+          best_cost = cost;
+          best = b;
+        }
+      }
+      used |= 1u << best;
+      pos[n] = 32 * g + best;
+      for (int32_t k = next->row_off[n]; k < next->row_off[n + 1]; ++k)
+        load[(size_t)gnext[next->cols[k]] * 32 + best]++;
+    }
+  }
+  return pos;
+}
 
 bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedLayer& out) {
   if (Q <= 0 || Q % 32 != 0 || N % Q != 0 || (scale != 1 && scale != 4)) return false;
@@ -99,7 +248,7 @@ bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedL
   out.max_depth = 0;
   out.slots = 0;
 
-  SlotSet lane_used[32], bank_used[32];
+  EdgeColoring coloring(64);
   struct Edge {
     int32_t lane, jl;
     float w;
@@ -124,25 +273,22 @@ bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedL
           ++cur[l];
         }
       }
-      for (int l = 0; l < 32; ++l) {
-        lane_used[l].clear();
-        bank_used[l].clear();
+      // Delta = max(lane degree, bank load): the colouring uses exactly that many slots
+      int lane_deg[32] = {0}, bank_load[32] = {0};
+      for (const Edge& e : edges) {
+        lane_deg[e.lane]++;
+        bank_load[e.jl & 31]++;
       }
+      int delta = 0;
+      for (int i = 0; i < 32; ++i) delta = std::max({delta, lane_deg[i], bank_load[i]});
+      coloring.reset(std::max(delta, 1));
       int32_t depth = 0;
       for (Edge& e : edges) {
-        const int bank = e.jl & 31;
-        int s = -1;
-        for (size_t wi = 0;; ++wi) {
-          const uint64_t m = lane_used[e.lane].word(wi) | bank_used[bank].word(wi);
-          if (m != ~0ull) {
-            s = (int)(wi * 64 + __builtin_ctzll(~m));
-            break;
-          }
-        }
-        e.slot = s;
-        lane_used[e.lane].set(s);
-        bank_used[bank].set(s);
-        depth = std::max(depth, s + 1);
+        coloring.add(e.lane, e.jl & 31);
+      }
+      for (size_t k = 0; k < edges.size(); ++k) {
+        edges[k].slot = coloring.colour((int)k);
+        depth = std::max(depth, edges[k].slot + 1);
       }
       out.max_depth = std::max(out.max_depth, depth);
       out.slots += depth;

@@ -41,4 +41,22 @@ struct PackedLayer {
 // returns false when (Q + 32) * scale does not fit 16 bits or Q is invalid.
 bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedLayer& out);
 
+// Same, with neurons placed at positions: input j of the layer is read from
+// position in_pos[j] of the incoming row and output c is written to position
+// out_pos[c] (nullptr = identity).
+bool pack_layer_placed(const HostLayer& h, int32_t N, int32_t Q, int32_t scale,
+                       const int32_t* in_pos, const int32_t* out_pos, PackedLayer& out);
+
+// Output grouping of a layer: outputs sorted by in-degree (descending, ties by
+// index); group g of the packed layout is order[32g .. 32g+31].
+std::vector<int32_t> degree_order(const HostLayer& h, int32_t N);
+
+// Positions of the outputs of a layer (whose grouping is `order`): each group
+// keeps its 32 outputs, and their lanes (= shared-memory banks in the next
+// layer) are chosen greedily so that every group of the next layer (grouping
+// next_order, weights next) sees balanced bank loads.  next == nullptr gives
+// lanes in order.
+std::vector<int32_t> place_outputs(const std::vector<int32_t>& order, const HostLayer* next,
+                                   const std::vector<int32_t>* next_order, int32_t N);
+
 }  // namespace sdnn

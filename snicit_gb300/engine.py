@@ -21,7 +21,7 @@ class Engine:
 
     def __init__(self, num_neurons=1024, num_layers=120, mode="SNICIT", threshold=30,
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
-                 device=0, tile_rows=0, threads=0, binary_first_layer=True):
+                 device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -37,7 +37,8 @@ class Engine:
         cfg.device = int(device)
         cfg.tile_rows = int(tile_rows)
         cfg.threads = int(threads)
-        cfg.reserved[0] = 0 if binary_first_layer else 1
+        cfg.flags = ((0 if binary_first_layer else _lib.FLAG_NO_BINARY_FIRST_LAYER)
+                     | (0 if placement else _lib.FLAG_NO_PLACEMENT))
         self.cfg = cfg
         self.N = cfg.num_neurons
         self.L = cfg.num_layers
@@ -130,6 +131,11 @@ class Engine:
             "pre_row_layers": s.pre_row_layers, "post_row_layers": s.post_row_layers,
             "weight_nnz": s.weight_nnz,
         }
+
+    def layer_rows(self):
+        out = np.zeros(self.L, dtype=np.int64)
+        self._ck(load().sdnn_get_layer_rows(self._h, _ptr(out), self.L))
+        return out
 
     def autotune(self, Y0, record_path=None):
         Y0 = np.ascontiguousarray(Y0, dtype=np.float32)

@@ -278,3 +278,21 @@ def test_binary_first_layer_is_bitwise_equal(N, L, B):
     assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
     Yref, alive, Y32 = _ref(_layers(N, L, seed), N, sg.load().sdnn_reference_bias(N), Y0)
     _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"bits N={N}", Y32=Y32)
+
+
+@pytest.mark.parametrize("mode", ["SNIG", "SNICIT"])
+def test_placement_gives_same_results(mode):
+    """Neuron placement only reorders the layout: categories identical, activations
+    within tolerance of each other and of the oracle (summation order differs)."""
+    N, L, B, seed = 1024, 14, 300, 77
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    res = {}
+    for place in (True, False):
+        with sg.Engine(N, L, mode=mode, threshold=5, batch=B, bias=-0.3, placement=place) as eng:
+            eng.generate_weights(seed)
+            flags, ids = eng.infer(Y0)
+            res[place] = (flags, ids, eng.activations(B))
+    assert np.array_equal(res[True][1], res[False][1])
+    Yref, alive, Y32 = _ref(_layers(N, L, seed), N, -0.3, Y0)
+    for place in (True, False):
+        _check(res[place][2], res[place][0], res[place][1], Yref, alive, f"place={place}", Y32=Y32)
