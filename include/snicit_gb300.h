@@ -188,6 +188,23 @@ int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
  * debugging output, src/SDGC/XY/XY.hpp:481.) */
 int sdnn_get_layer_rows(const sdnn_engine* e, int64_t* out, int32_t num_layers);
 
+/* One plain layer (bias + ReLU + clamp) of an engine whose weights are already
+ * on the device, applied to `rows` caller-owned rows: d_y_in (rows x N FP32,
+ * 16-byte aligned) -> d_y_out (rows x N), d_alive[r] = 1 if row r has an
+ * output > 0.  Allocates no memory at all; has no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc (during CUDA-graph
+ * capture, fixed-budget or real-time serving threads, hosts whose allocator
+ * belongs to another framework).  Its scratch is a static device array for
+ * at most 65536 rows (larger `rows` -> SDNN_ERR_INVALID), shared by all calls
+ * on a device: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make it before
+ * any stream capture.  Rows are in the engine's storage order: neuron order
+ * for layer 0's input, and for every layer when the engine was created with
+ * SDNN_FLAG_NO_PLACEMENT.  Requires sdnn_finalize_weights (or an inference)
+ * first; stream NULL = the engine's stream; does not synchronise. */
+int sdnn_layer_noalloc(sdnn_engine* e, int32_t layer, const float* d_y_in, float* d_y_out,
+                       int64_t rows, int32_t* d_alive, void* stream);
+
 /* Chooses threshold, centroid count and tile shape by timing the candidates
  * on the given sample rows (host buffer) and appends one JSON line per tried
  * setting to record_path (if not NULL).  Applies the fastest setting. */

@@ -72,6 +72,7 @@ SIGNATURES = [
     ("sdnn_get_stats", ctypes.c_int, [P, P]),
     ("sdnn_get_layer_rows", ctypes.c_int, [P, P, I32]),
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
+    ("sdnn_layer_noalloc", ctypes.c_int, [P, I32, P, P, I64, P, P]),
     ("sdnn_generate_inputs", ctypes.c_int, [I32, U64, I64, I64, P]),
     ("sdnn_generate_layer_coo", ctypes.c_int, [I32, U64, I32, I32, F32, P, P, P]),
     ("sdnn_write_weights_tsv", ctypes.c_int, [P, ctypes.c_char_p]),

@@ -1081,4 +1081,45 @@ void engine_set_snicit(sdnn_engine* e, int threshold, int centroids) {
   drop_graph(e);
 }
 sdnn_config engine_config(const sdnn_engine* e) { return e->cfg; }
+
+// Fills the weight/shape part of the layer-kernel arguments of `layer` and the
+// launch shape, without allocating anything: the weights must already be on
+// the device (sdnn_finalize_weights or an earlier inference).
+int engine_layer_setup(sdnn_engine* e, int layer, LayerArgs* a, LayerKernelKey* key, int* grid,
+                       int* threads, size_t* smem) {
+  if (layer < 0 || layer >= e->L) return fail(e, SDNN_ERR_INVALID, "bad layer");
+  if (!e->stream || e->weights_dirty || (int)e->dl.size() != e->L)
+    return fail(e, SDNN_ERR_STATE, "weights are not on the device: call sdnn_finalize_weights first");
+  CK(cudaSetDevice(e->dev));
+  if (e->grid == 0) {
+    int rc = choose_kernel(e);
+    if (rc) return rc;
+  }
+  const DevLayer& d = e->dl[layer];
+  LayerKernelKey k = e->key;
+  k.constw = d.constw;
+  CK(layer_prepare(k, e->smem));
+  *a = LayerArgs{};
+  a->w.idx = d.idx;
+  a->w.val = d.val;
+  a->w.grp_blk = d.grp;
+  a->w.bias_vec = d.bias;
+  a->w.bias = e->cfg.bias;
+  a->w.wconst = d.wconst;
+  a->N = e->N;
+  a->nq = e->nq;
+  a->Q = e->Q;
+  a->G = e->G;
+  a->epi = EPI_PLAIN;
+  a->max_split = e->G;
+  a->min_split = e->min_split;
+  a->clampv = e->cfg.clamp;
+  *key = k;
+  *grid = d.constw ? e->grid : e->grid_general;
+  *threads = e->threads;
+  *smem = e->smem;
+  return SDNN_OK;
+}
+cudaStream_t engine_stream(const sdnn_engine* e) { return e->stream; }
+void engine_set_error(sdnn_engine* e, const std::string& msg) { e->err = msg; }
 }  // namespace sdnn
