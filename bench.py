@@ -186,16 +186,17 @@ def run_ours(args):
     edges = float(B) * NNZ * N * L
 
     eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=B, bias=bias,
-                    num_centroids=args.centroids, device=local)
+                    num_centroids=args.centroids, device=local, tile_rows=args.tile,
+                    threads=args.threads)
     eng.generate_weights(SEED, NNZ, 0.0625)
     eng.finalize()
     tune = None
-    if not args.no_autotune:
+    if not args.no_autotune and not args.tile:
         rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
         os.makedirs(os.path.dirname(rec), exist_ok=True)
         if os.path.exists(rec):
             os.remove(rec)
-        tune = eng.autotune(Y0[: args.tune_rows], rec)
+        tune = eng.autotune(Y0[: args.tune_rows] if args.tune_rows else Y0, rec)
 
     d_in = torch.from_numpy(Y0).to(f"cuda:{local}")
     d_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
@@ -247,8 +248,8 @@ def run_ours(args):
 
     # plain per-layer path on the same batch (the comparison point)
     plain = sg.Engine(N, L, mode="SNIG", batch=B, bias=bias, device=local,
-                      tile_rows=tune["tile_rows"] if tune else 0,
-                      threads=tune["threads"] if tune else 0)
+                      tile_rows=tune["tile_rows"] if tune else args.tile,
+                      threads=tune["threads"] if tune else args.threads)
     plain.generate_weights(SEED, NNZ, 0.0625)
     plain_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
     for _ in range(2):
@@ -348,7 +349,9 @@ def main():
     ap.add_argument("--workload", default="sdgc-4096x480", choices=sorted(WORKLOADS))
     ap.add_argument("--threshold", type=int, default=None)
     ap.add_argument("--centroids", type=int, default=50)
-    ap.add_argument("--tune-rows", type=int, default=16384)
+    ap.add_argument("--tune-rows", type=int, default=0, help="rows used by the autotuner (0 = all)")
+    ap.add_argument("--tile", type=int, default=0, help="fix the layer-kernel tile rows (skips autotune)")
+    ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

@@ -82,6 +82,8 @@ typedef struct sdnn_config {
  * either way; used to compare the paths). */
 #define SDNN_FLAG_NO_BINARY_FIRST_LAYER 1  /* float kernel for layer 0 even for 0/1 inputs */
 #define SDNN_FLAG_NO_PLACEMENT 2           /* keep neuron order; no degree/bank placement   */
+#define SDNN_FLAG_NO_CHAIN 4               /* SNICIT: per-layer post launches even when no  */
+                                           /* residue row is left                           */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -164,8 +166,11 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows,
                     int32_t* flags, int32_t* ids, int64_t* count);
 
 /* Device-resident inference on the engine's stream (cudaStream_t passed as
- * void*; NULL = the engine's own).  d_Y0 rows x N FP32 device pointer,
- * d_flags rows int32 device pointer.  Does not synchronize. */
+ * void*; NULL = the engine's own).  d_Y0 rows x N FP32 device pointer
+ * (16-byte aligned), d_flags rows int32 device pointer.  Plain modes do not
+ * synchronize; SNICIT waits once, after the threshold clustering, to read how
+ * many residue rows and centroids it produced (which picks the kernels for the
+ * remaining layers). */
 int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
                       int32_t* d_flags, void* stream);
 

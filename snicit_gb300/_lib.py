@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(PKG, "libsnicit_gb300.so")
 MODES = {"BF": 0, "SNIG": 1, "XY": 2, "SNICIT": 3}
 FLAG_NO_BINARY_FIRST_LAYER = 1
 FLAG_NO_PLACEMENT = 2
+FLAG_NO_CHAIN = 4
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",

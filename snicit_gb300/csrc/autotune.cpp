@@ -69,8 +69,8 @@ extern "C" int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows,
   const sdnn_config cfg0 = sdnn::engine_config(e);
   const int N = cfg0.num_neurons;
   std::vector<int> tiles;
-  if (N == 1024) tiles = {32, 24, 16, 8};
-  else if (N == 4096) tiles = {12, 8, 6, 4, 2};
+  if (N == 1024) tiles = {24, 16, 12, 8};
+  else if (N == 4096) tiles = {6, 5, 4, 3, 2};
   else if (N == 16384) tiles = {3, 2, 1};
   else if (N > 32768) tiles = {3, 2, 1};
   else tiles = {8, 4, 2, 1};

@@ -45,6 +45,23 @@ struct DevLayer {
   int32_t max_depth = 0;
 };
 
+struct GraphKey {
+  int64_t rows = -1;
+  const float* in = nullptr;
+  int32_t* flags = nullptr;
+  int T = -1, K = -1, mode = -1, tile = -1, threads = -1, chain_kc = -1;
+  bool operator==(const GraphKey& o) const {
+    return rows == o.rows && in == o.in && flags == o.flags && T == o.T && K == o.K &&
+           mode == o.mode && tile == o.tile && threads == o.threads && chain_kc == o.chain_kc;
+  }
+};
+
+struct GraphSlot {
+  cudaGraphExec_t exec = nullptr;
+  GraphKey key;
+  int launches = 0;
+};
+
 struct GenSpec {
   bool on = false;
   uint64_t seed = 0;
@@ -110,12 +127,14 @@ struct sdnn_engine {
 
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
-  // graph cache
-  cudaGraphExec_t gexec = nullptr;
-  int64_t g_rows = -1;
-  const float* g_in = nullptr;
-  int32_t* g_flags = nullptr;
-  int g_T = -1, g_K = -1, g_mode = -1, g_tile = -1, g_threads = -1;
+  // graph cache: one captured graph per phase of an inference
+  GraphSlot graphs[5];
+  int run_launches = 0;
+  int32_t* h_counts = nullptr;  // pinned: residue rows and centroids after clustering
+  int chain_cap = 0;            // centroid rows the cluster chain kernel can carry
+  int chain_kc = 1;
+  bool last_chain = false;
+  LayerDev* d_layer_table = nullptr;  // device copy of every layer's descriptor
 
   // last run
   int64_t last_rows = 0;
@@ -149,6 +168,7 @@ void dfree(T*& p) {
 
 void free_weights(sdnn_engine* e) {
   dfree(e->d_perm_final);
+  dfree(e->d_layer_table);
   for (auto& d : e->dl) {
     dfree(d.idx);
     dfree(d.val);
@@ -187,16 +207,25 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_in);
   dfree(e->d_fallback);
   dfree(e->d_fbcount);
+  if (e->h_counts) cudaFreeHost(e->h_counts);
+  e->h_counts = nullptr;
   e->cap = 0;
 }
 
 void drop_graph(sdnn_engine* e) {
-  if (e->gexec) cudaGraphExecDestroy(e->gexec);
-  e->gexec = nullptr;
-  e->g_rows = -1;
+  for (auto& g : e->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = GraphSlot{};
+  }
 }
 
 constexpr size_t kMaxSmem = 227 * 1024;
+// threads per CTA of the binary first-layer kernel: small enough for two or
+// three CTAs per SM, so one CTA's row loads overlap another's counting
+#ifndef SDNN_BITS_THREADS
+#define SDNN_BITS_THREADS 256
+#endif
+constexpr int kBitsThreads = SDNN_BITS_THREADS;
 
 // Chooses chunking, kernel instance, tile rows, threads and grid.
 // Input chunking of the weight layout: whole rows up to 32768 neurons, else
@@ -217,8 +246,8 @@ int choose_kernel(sdnn_engine* e) {
   if (e->nq == 1) {
     int rsw = e->Q == 1024 ? 1056 : e->Q == 4096 ? 4128 : e->Q == 16384 ? 16416 : 0;
     std::vector<int> Ts;
-    if (rsw == 1056) Ts = {32, 24, 16, 8};
-    else if (rsw == 4128) Ts = {8, 12, 6, 4, 2};
+    if (rsw == 1056) Ts = {16, 12, 24, 8};
+    else if (rsw == 4128) Ts = {3, 6, 4, 5, 2};
     else if (rsw == 16416) Ts = {3, 2, 1};
     else Ts = {8, 4, 2, 1};
     for (int T : Ts) cands.push_back({T, rsw, 1, true});
@@ -233,7 +262,7 @@ int choose_kernel(sdnn_engine* e) {
   }
   for (const auto& k : cands) {
     if (req_T > 0 && k.T != req_T) continue;
-    const size_t smem = (size_t)k.T * (size_t)(e->Q + 32) * 4;
+    const size_t smem = (size_t)layer_buffers(k.kg, k.rsw) * k.T * (size_t)(e->Q + 32) * 4;
     if (smem > kMaxSmem) continue;
     if (!layer_instance_exists(k)) continue;
     LayerKernelKey kc = k, kg = k;
@@ -298,6 +327,7 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
   T(A(&e->d_fbcount, 16));
+  if (rc == cudaSuccess) T(cudaMallocHost((void**)&e->h_counts, 16));
   if (rc != cudaSuccess) {
     free_buffers(e);
     cudaGetLastError();
@@ -461,6 +491,21 @@ int finalize_weights(sdnn_engine* e) {
     free_weights(e);
     return rc;
   }
+  {
+    std::vector<LayerDev> table(e->L);
+    for (int l = 0; l < e->L; ++l) {
+      const DevLayer& d = e->dl[l];
+      table[l].idx = d.idx;
+      table[l].val = d.val;
+      table[l].grp_blk = d.grp;
+      table[l].bias_vec = d.bias;
+      table[l].bias = e->cfg.bias;
+      table[l].wconst = d.wconst;
+    }
+    CK(cudaMalloc((void**)&e->d_layer_table, sizeof(LayerDev) * e->L));
+    CK(cudaMemcpy(e->d_layer_table, table.data(), sizeof(LayerDev) * e->L, cudaMemcpyHostToDevice));
+  }
+  e->chain_cap = e->nq == 1 ? chain_capacity(e->N) : 0;
   if (!e->pos.empty()) {
     CK(cudaMalloc((void**)&e->d_perm_final, (size_t)e->N * 4));
     CK(cudaMemcpy(e->d_perm_final, e->pos[e->L - 1].data(), (size_t)e->N * 4,
@@ -523,20 +568,18 @@ int effective_threshold(const sdnn_engine* e) {
   return std::max(0, std::min(e->cfg.threshold, e->L));
 }
 
-// Enqueues one inference of `rows` rows read from d_in, flags to d_flags.
-int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, bool capturing) {
+// Parts of one inference.  Plain modes (and thresholds at or past the last
+// layer) enqueue PH_ALL.  SNICIT runs PH_PRE (plain layers below the threshold
+// and the clustering), then, depending on what the clustering left (read back
+// by the host once), PH_POST_CHAIN (no residue rows: the centroid rows alone,
+// one cluster kernel for all remaining layers) or PH_POST_LAYERS (a centroid
+// and a residue launch per layer), then PH_FINISH (recovery).
+enum Phase { PH_ALL = 0, PH_PRE = 1, PH_POST_LAYERS = 2, PH_POST_CHAIN = 3, PH_FINISH = 4 };
+
+int enqueue_plain_layers(sdnn_engine* e, int64_t rows, const float* d_in, int T, bool capturing) {
   const int L = e->L;
-  const int T = effective_threshold(e);
-  const size_t N = (size_t)e->N;
   const cudaStream_t s = e->stream;
-  e->launches = 0;
   int rc;
-  if ((rc = record(e, 0, capturing))) return rc;
-  CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
-  CK(cudaMemsetAsync(d_flags, 0, (size_t)rows * 4, s));
-  CK(cudaMemsetAsync(e->d_state, 0, (size_t)rows * 4, s));
-  launch_iota(e->d_list[0], e->d_counts, (int32_t)rows, s);
-  e->launches++;
   // XY mode splits the plain loop at the threshold for its pre/post timing
   // (src/SDGC/XY/XY.hpp:492-501); BF and SNIG time the loop as one stage.
   const int split = e->cfg.mode == SDNN_MODE_XY ? std::max(0, std::min(e->cfg.threshold, L)) : T;
@@ -566,7 +609,7 @@ int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, b
       b.fallback_count = e->d_fbcount;
       b.N = e->N;
       b.G = e->G;
-      CK(launch_layer0_bits(b, e->bits_grid, 512, s));
+      CK(launch_layer0_bits(b, e->bits_grid, kBitsThreads, s));
       e->launches++;
       if ((rc = layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount,
                              e->d_list[1], e->d_counts + 1)))
@@ -580,11 +623,31 @@ int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, b
   if (!(split < T && T == L)) {
     if ((rc = record(e, 1, capturing))) return rc;
   }
-  if (T < L) {
-    float* ybuf = e->d_y[(T - 1 + 2) & 1];
+  return SDNN_OK;
+}
+
+// Enqueues one phase of an inference of `rows` rows read from d_in.
+int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t* d_flags,
+            bool capturing) {
+  const int L = e->L;
+  const int T = effective_threshold(e);
+  const size_t N = (size_t)e->N;
+  const cudaStream_t s = e->stream;
+  int rc;
+  float* ybuf = e->d_y[(T - 1 + 2) & 1];  // activations at the threshold
+  const int32_t* live = e->d_list[T & 1];
+  const int32_t* live_count = e->d_counts + T;
+  if (phase == PH_ALL || phase == PH_PRE) {
+    if ((rc = record(e, 0, capturing))) return rc;
+    CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
+    CK(cudaMemsetAsync(d_flags, 0, (size_t)rows * 4, s));
+    CK(cudaMemsetAsync(e->d_state, 0, (size_t)rows * 4, s));
+    launch_iota(e->d_list[0], e->d_counts, (int32_t)rows, s);
+    e->launches++;
+    if ((rc = enqueue_plain_layers(e, rows, d_in, T, capturing))) return rc;
+  }
+  if (phase == PH_PRE) {
     if (T == 0) CK(cudaMemcpyAsync(ybuf, d_in, (size_t)rows * N * 4, cudaMemcpyDeviceToDevice, s));
-    const int32_t* live = e->d_list[T & 1];
-    const int32_t* live_count = e->d_counts + T;
     CK(cudaMemsetAsync(e->d_rcounts, 0, (size_t)(L + 4) * 4, s));
     CK(cudaMemsetAsync(e->d_iscent, 0, (size_t)rows * 4, s));
     CK(cudaMemsetAsync(e->d_resflag, 0, (size_t)rows * 4, s));
@@ -610,6 +673,8 @@ int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, b
     launch_cluster(c, e->num_sms, s);
     e->launches += 4;
     if ((rc = record(e, 2, capturing))) return rc;
+  }
+  if (phase == PH_POST_LAYERS) {
     for (int l = T; l < L; ++l) {
       const int p = l - T;
       const float* in = e->d_y[(l - 1 + 2) & 1];
@@ -622,68 +687,119 @@ int enqueue(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags, b
         return rc;
     }
     if ((rc = record(e, 3, capturing))) return rc;
+  }
+  if (phase == PH_POST_CHAIN) {
+    ChainArgs ca{};
+    ca.layers = e->d_layer_table;
+    ca.first = T;
+    ca.last = L;
+    ca.y_in = ybuf;
+    ca.y_out = e->d_y[(L - 1) & 1];
+    ca.clist = e->d_clist;
+    ca.ccount = e->d_ccount;
+    ca.N = e->N;
+    ca.G = e->G;
+    ca.clampv = e->cfg.clamp;
+    CK(launch_chain(ca, e->chain_kc, s));
+    e->launches++;
+    if ((rc = record(e, 3, capturing))) return rc;
+  }
+  if (phase == PH_FINISH) {
     const int pf = L - T;
     launch_mark_rows(e->d_rlist[pf & 1], e->d_rcounts + pf, e->d_resflag, 1, s);
     launch_recover(e->d_y[(L - 1) & 1], live, live_count, e->d_cslot, e->d_clist, e->d_iscent,
                    e->d_resflag, e->N, d_flags, s);
     launch_mark_rows(live, live_count, e->d_state, 2, s);
     e->launches += 3;
-  } else {
-    if (!(split < T)) {
+    if ((rc = record(e, 4, capturing))) return rc;
+  }
+  if (phase == PH_ALL) {
+    if (e->cfg.mode != SDNN_MODE_XY || std::min(e->cfg.threshold, L) >= T) {
       if ((rc = record(e, 2, capturing))) return rc;
     }
     if ((rc = record(e, 3, capturing))) return rc;
     launch_identify(e->d_y[(L - 1) & 1], e->d_list[L & 1], e->d_counts + L, e->N, d_flags, s);
     launch_mark_rows(e->d_list[L & 1], e->d_counts + L, e->d_state, 1, s);
     e->launches += 2;
+    if ((rc = record(e, 4, capturing))) return rc;
   }
-  if ((rc = record(e, 4, capturing))) return rc;
   CK(cudaGetLastError());
+  return SDNN_OK;
+}
+
+// Runs one phase: eagerly in BF mode, else from a cached CUDA graph (captured
+// on first use and whenever the pointers, sizes or kernel choice change).
+int run_phase(sdnn_engine* e, int slot, int phase, int64_t rows, const float* d_in,
+              int32_t* d_flags) {
+  if (e->cfg.mode == SDNN_MODE_BF) {
+    const int before = e->launches;
+    e->launches = 0;
+    int rc = enqueue(e, phase, rows, d_in, d_flags, false);
+    e->run_launches += e->launches;
+    e->launches = before;
+    return rc;
+  }
+  GraphSlot& g = e->graphs[slot];
+  const GraphKey key{rows, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
+                     e->key.T, e->threads, phase == PH_POST_CHAIN ? e->chain_kc : 0};
+  if (!g.exec || !(g.key == key)) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+    e->launches = 0;
+    CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue(e, phase, rows, d_in, d_flags, true);
+    cudaGraph_t graph = nullptr;
+    cudaError_t rc2 = cudaStreamEndCapture(e->stream, &graph);
+    if (rc != SDNN_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return rc;
+    }
+    if (rc2 != cudaSuccess) return cuda_fail(e, rc2, "cudaStreamEndCapture");
+    cudaError_t rc3 = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc3 != cudaSuccess) {
+      g.exec = nullptr;
+      return cuda_fail(e, rc3, "cudaGraphInstantiate");
+    }
+    g.key = key;
+    g.launches = e->launches;
+  }
+  CK(cudaGraphLaunch(g.exec, e->stream));
+  e->run_launches += g.launches;
   return SDNN_OK;
 }
 
 int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   if (rows <= 0) return fail(e, SDNN_ERR_INVALID, "rows must be positive");
   if (rows > e->cap) return fail(e, SDNN_ERR_INVALID, "rows exceed the batch capacity");
-  const bool graph = e->cfg.mode != SDNN_MODE_BF;
   const int T = effective_threshold(e);
   e->last_T = T;
   e->last_rows = rows;
-  if (!graph) {
-    int rc = enqueue(e, rows, d_in, d_flags, false);
-    if (rc) return rc;
+  e->run_launches = 0;
+  int rc;
+  if (e->cfg.mode != SDNN_MODE_SNICIT || T >= e->L) {
+    if ((rc = run_phase(e, 0, PH_ALL, rows, d_in, d_flags))) return rc;
   } else {
-    if (!e->gexec || e->g_rows != rows || e->g_in != d_in || e->g_flags != d_flags ||
-        e->g_T != T || e->g_K != e->Kmax || e->g_mode != e->cfg.mode ||
-        e->g_tile != e->key.T || e->g_threads != e->threads) {
-      drop_graph(e);
-      CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = enqueue(e, rows, d_in, d_flags, true);
-      cudaGraph_t g = nullptr;
-      cudaError_t rc2 = cudaStreamEndCapture(e->stream, &g);
-      if (rc != SDNN_OK) {
-        if (g) cudaGraphDestroy(g);
-        cudaGetLastError();
-        return rc;
-      }
-      if (rc2 != cudaSuccess) return cuda_fail(e, rc2, "cudaStreamEndCapture");
-      cudaError_t rc3 = cudaGraphInstantiate(&e->gexec, g, 0);
-      cudaGraphDestroy(g);
-      if (rc3 != cudaSuccess) {
-        e->gexec = nullptr;
-        return cuda_fail(e, rc3, "cudaGraphInstantiate");
-      }
-      e->g_rows = rows;
-      e->g_in = d_in;
-      e->g_flags = d_flags;
-      e->g_T = T;
-      e->g_K = e->Kmax;
-      e->g_mode = e->cfg.mode;
-      e->g_tile = e->key.T;
-      e->g_threads = e->threads;
+    if ((rc = run_phase(e, 1, PH_PRE, rows, d_in, d_flags))) return rc;
+    // what did the clustering leave?  (one small read-back per inference)
+    CK(cudaMemcpyAsync(e->h_counts, e->d_rcounts, 4, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(e->h_counts + 1, e->d_ccount, 4, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    const int residues = e->h_counts[0], centroids = e->h_counts[1];
+    const bool chain = e->chain_cap > 0 && residues == 0 && centroids >= 1 &&
+                       centroids <= e->chain_cap && !(e->cfg.flags & SDNN_FLAG_NO_CHAIN);
+    if (chain) {
+      e->chain_kc = 1;
+      while (e->chain_kc < centroids) e->chain_kc *= 2;
+      if ((rc = run_phase(e, 2, PH_POST_CHAIN, rows, d_in, d_flags))) return rc;
+    } else {
+      if ((rc = run_phase(e, 3, PH_POST_LAYERS, rows, d_in, d_flags))) return rc;
     }
-    CK(cudaGraphLaunch(e->gexec, e->stream));
+    e->last_chain = chain;
+    if ((rc = run_phase(e, 4, PH_FINISH, rows, d_in, d_flags))) return rc;
   }
+  e->launches = e->run_launches;
   e->have_run = true;
   e->pending_stats = 1;
   return SDNN_OK;
@@ -714,7 +830,7 @@ int prepare(sdnn_engine* e, int64_t rows) {
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
   e->bits_grid = (e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
                   layer0_bits_supported(e->N))
-                     ? layer0_bits_grid(e->N, e->num_sms, 512)
+                     ? layer0_bits_grid(e->N, e->num_sms, kBitsThreads)
                      : 0;
   return ensure_buffers(e, rows);
 }

@@ -32,7 +32,7 @@ __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32
 }
 
 template <int RSW>
-__global__ void __launch_bounds__(512, 1) layer0_bits_kernel(const Layer0Args a) {
+__global__ void __launch_bounds__(512) layer0_bits_kernel(const Layer0Args a) {
   extern __shared__ __align__(128) uint32_t bits[];  // RSW words
   __shared__ float s_sum[128];
   __shared__ int32_t s_rows[32];

@@ -76,56 +76,80 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 __device__ __forceinline__ float clampf(float v, float hi) { return fminf(hi, fmaxf(0.f, v)); }
 
+// Applies NB blocks of slots (indices in iv, values in vv) to acc[T].
+template <int T, int RSW, bool CONSTW, int NB>
+__device__ __forceinline__ void apply_blocks(float (&acc)[T], const uint2 (&iv)[NB],
+                                             const float4 (&vv)[CONSTW ? 1 : NB], float wc,
+                                             const float* __restrict__ ys, int RS) {
+#pragma unroll
+  for (int k = 0; k < NB; ++k) {
+    const uint32_t words[2] = {iv[k].x, iv[k].y};
+    float wv[4];
+    if constexpr (!CONSTW) {
+      wv[0] = vv[k].x; wv[1] = vv[k].y; wv[2] = vv[k].z; wv[3] = vv[k].w;
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const uint32_t j = (words[s >> 1] >> ((s & 1) * 16)) & 0xffffu;
+      // byte offset or float index, fixed by the packer for this row stride
+      const float* p = rsw_in_bytes(RSW)
+                           ? reinterpret_cast<const float*>(reinterpret_cast<const char*>(ys) + j)
+                           : ys + j;
+      const float w = CONSTW ? wc : wv[s];
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const int off = (RSW > 0 ? RSW : RS) * t;
+        acc[t] = fmaf(w, p[off], acc[t]);
+      }
+    }
+  }
+}
+
+// Loads NB blocks starting at block b (indices and, for general layers, values).
+template <bool CONSTW, int NB>
+__device__ __forceinline__ void load_blocks(uint2 (&iv)[NB], float4 (&vv)[CONSTW ? 1 : NB],
+                                            const uint2* __restrict__ ip,
+                                            const float4* __restrict__ vp, int b) {
+#pragma unroll
+  for (int k = 0; k < NB; ++k) {
+    iv[k] = __ldg(ip + (size_t)(b + k) * 32);
+    if constexpr (!CONSTW) vv[k] = __ldg(vp + (size_t)(b + k) * 32);
+  }
+}
+
 // Accumulates the in-edges of group g from input chunk q into acc[T].
-// The slot indices (and values) of up to PF blocks are loaded into registers
-// before any of them is used, so a warp waits for one memory round trip per
-// PF blocks instead of one per block (the post-threshold launches have one
-// warp per group and nothing else to hide that latency).
+// Slot blocks are fetched in batches of 8, then 2, then 1 (no predicated
+// tail): all indices of a batch are in registers before the first is used,
+// so a warp waits for one memory round trip per batch (the post-threshold
+// launches have one warp per group and nothing else to hide that latency).
 template <int T, int RSW, bool CONSTW>
-__device__ __forceinline__ void accumulate_group(float (&acc)[T], const LayerArgs& a,
+__device__ __forceinline__ void accumulate_group(float (&acc)[T], const LayerDev& wl, int nq,
                                                  const float* __restrict__ ys, int RS, int g,
                                                  int q, int lane) {
-  constexpr int PF = CONSTW ? 16 : 8;
-  const int32_t b0 = __ldg(a.w.grp_blk + g * a.nq + q);
-  const int32_t b1 = __ldg(a.w.grp_blk + g * a.nq + q + 1);
-  const uint2* __restrict__ ip = a.w.idx + (size_t)b0 * 32 + lane;
-  const float4* __restrict__ vp = CONSTW ? nullptr : a.w.val + (size_t)b0 * 32 + lane;
-  const float wc = a.w.wconst;
+  const int32_t b0 = __ldg(wl.grp_blk + g * nq + q);
+  const int32_t b1 = __ldg(wl.grp_blk + g * nq + q + 1);
+  const uint2* __restrict__ ip = wl.idx + (size_t)b0 * 32 + lane;
+  const float4* __restrict__ vp = CONSTW ? nullptr : wl.val + (size_t)b0 * 32 + lane;
+  const float wc = wl.wconst;
   const int nb = b1 - b0;
-  for (int bb = 0; bb < nb; bb += PF) {
-    uint2 iv[PF];
-    float4 vv[CONSTW ? 1 : PF];
-#pragma unroll
-    for (int k = 0; k < PF; ++k) {
-      if (bb + k < nb) {
-        iv[k] = __ldg(ip + (size_t)(bb + k) * 32);
-        if constexpr (!CONSTW) vv[k] = __ldg(vp + (size_t)(bb + k) * 32);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < PF; ++k) {
-      if (bb + k < nb) {
-        const uint32_t words[2] = {iv[k].x, iv[k].y};
-        float wv[4];
-        if constexpr (!CONSTW) {
-          wv[0] = vv[k].x; wv[1] = vv[k].y; wv[2] = vv[k].z; wv[3] = vv[k].w;
-        }
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const uint32_t j = (words[s >> 1] >> ((s & 1) * 16)) & 0xffffu;
-          // byte offset or float index, fixed by the packer for this row stride
-          const float* p = rsw_in_bytes(RSW)
-                               ? reinterpret_cast<const float*>(reinterpret_cast<const char*>(ys) + j)
-                               : ys + j;
-          const float w = CONSTW ? wc : wv[s];
-#pragma unroll
-          for (int t = 0; t < T; ++t) {
-            const int off = (RSW > 0 ? RSW : RS) * t;
-            acc[t] = fmaf(w, p[off], acc[t]);
-          }
-        }
-      }
-    }
+  int b = 0;
+  for (; b + 8 <= nb; b += 8) {
+    uint2 iv[8];
+    float4 vv[CONSTW ? 1 : 8];
+    load_blocks<CONSTW, 8>(iv, vv, ip, vp, b);
+    apply_blocks<T, RSW, CONSTW, 8>(acc, iv, vv, wc, ys, RS);
+  }
+  for (; b + 2 <= nb; b += 2) {
+    uint2 iv[2];
+    float4 vv[CONSTW ? 1 : 2];
+    load_blocks<CONSTW, 2>(iv, vv, ip, vp, b);
+    apply_blocks<T, RSW, CONSTW, 2>(acc, iv, vv, wc, ys, RS);
+  }
+  if (b < nb) {
+    uint2 iv[1];
+    float4 vv[1];
+    load_blocks<CONSTW, 1>(iv, vv, ip, vp, b);
+    apply_blocks<T, RSW, CONSTW, 1>(acc, iv, vv, wc, ys, RS);
   }
 }
 
@@ -168,29 +192,85 @@ __device__ __forceinline__ uint32_t epilogue_group(const float (&acc)[T], const 
   return m;
 }
 
+// Issues the TMA bulk copies of the rows of one tile (one input chunk) into a
+// shared buffer and arms its mbarrier; called by one thread.
+__device__ __forceinline__ void load_tile(const LayerArgs& a, float* buf, int RS,
+                                          const int32_t* rows, int nrows, int q, uint64_t* bar) {
+  const uint32_t row_bytes = (uint32_t)a.Q * 4u;
+  mbar_expect_tx(bar, row_bytes * (uint32_t)nrows);
+  for (int t = 0; t < nrows; ++t) {
+    const char* src =
+        reinterpret_cast<const char*>(a.y_in + (size_t)rows[t] * a.N + (size_t)q * a.Q);
+    char* dst = reinterpret_cast<char*>(buf + (size_t)t * RS);
+    for (uint32_t off = 0; off < row_bytes; off += 32768u)
+      bulk_g2s(dst + off, src + off, min(32768u, row_bytes - off), bar);
+  }
+}
+
+// Work split shared by all CTAs of a launch (same count, same grid).
+struct Split {
+  int count, n_tiles, spl;
+  long items;
+};
+template <int T>
+__device__ __forceinline__ Split make_split(const LayerArgs& a) {
+  Split sp;
+  sp.count = *a.count_in;
+  sp.n_tiles = (sp.count + T - 1) / T;
+  int spl = sp.n_tiles > 0 ? (int)((gridDim.x + sp.n_tiles - 1) / sp.n_tiles) : 1;
+  spl = max(spl, a.min_split);
+  spl = min(spl, a.max_split);
+  sp.spl = max(spl, 1);
+  sp.items = (long)sp.n_tiles * sp.spl;
+  return sp;
+}
+
+// Publishes the flagged rows of a finished item: straight to the next list,
+// or through the per-tile mask and ticket when several CTAs share the tile.
+template <int T>
+__device__ __forceinline__ void publish_rows(const LayerArgs& a, uint32_t m, int tile, int spl,
+                                             const int32_t* rows) {
+  if (a.epi == EPI_CENTROID) return;
+  bool emit = true;
+  if (spl > 1) {
+    atomicOr(a.tile_mask + tile, m);
+    __threadfence();
+    const int tk = atomicAdd(a.tile_ticket + tile, 1);
+    emit = (tk == spl - 1);
+    if (emit) {
+      __threadfence();
+      m = atomicExch(a.tile_mask + tile, 0u);
+      a.tile_ticket[tile] = 0;
+    }
+  }
+  if (emit && m) {
+    const int base = atomicAdd(a.count_out, __popc(m));
+    int i = 0;
+    for (int t = 0; t < T; ++t)
+      if (m & (1u << t)) a.list_out[base + i++] = rows[t];
+  }
+}
+
 template <int T, int RSW, int KG, bool CONSTW>
 __global__ void __launch_bounds__(512) layer_kernel(const LayerArgs a) {
   extern __shared__ __align__(128) float ys[];
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ int32_t s_rows[T];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int32_t s_rows[2][T];
   __shared__ uint32_t s_mask;
   __shared__ int32_t s_fail;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int RS = RSW > 0 ? RSW : a.Q + 32;
-  const int count = *a.count_in;
-  if (count <= 0) return;
-  const int n_tiles = (count + T - 1) / T;
-  int spl = (int)((gridDim.x + n_tiles - 1) / n_tiles);
-  spl = max(spl, a.min_split);
-  spl = min(spl, a.max_split);
-  spl = max(spl, 1);
-  const long items = (long)n_tiles * spl;
-  if ((long)blockIdx.x >= items) return;
-
-  for (int i = tid; i < T * 32; i += blockDim.x) ys[(i >> 5) * RS + a.Q + (i & 31)] = 0.f;
+  const Split sp = make_split<T>(a);
+  if (sp.count <= 0 || (long)blockIdx.x >= sp.items) return;
+  // Whole-row layouts of N = 1024 / 4096: two tile buffers (the next tile
+  // streams in while this one is computed); otherwise one buffer, reloaded per
+  // item and input chunk.
+  constexpr int NBUF = layer_buffers(KG, RSW);
+  for (int i = tid; i < NBUF * T * 32; i += blockDim.x) ys[(i >> 5) * RS + a.Q + (i & 31)] = 0.f;
   if (tid == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     s_mask = 0;
     s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -198,33 +278,79 @@ __global__ void __launch_bounds__(512) layer_kernel(const LayerArgs a) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
 
-  uint32_t phase = 0;
-  int loaded_tile = -1;
-  for (long item = blockIdx.x; item < items; item += gridDim.x) {
-    const int tile = (int)(item / spl), part = (int)(item % spl);
-    const int row0 = tile * T;
-    const int nrows = min(T, count - row0);
-    const int gbeg = (int)((long)a.G * part / spl), gend = (int)((long)a.G * (part + 1) / spl);
-    __syncthreads();
-    if (tid < T) s_rows[tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
-    __syncthreads();
-
-    if constexpr (KG == 1) {
+  if constexpr (NBUF == 2) {
+    // item k of this CTA is blockIdx.x + k * gridDim.x; buffer k & 1
+    auto item_rows = [&](long item, int32_t* rows) -> int {
+      const int tile = (int)(item / sp.spl);
+      const int row0 = tile * T;
+      const int nrows = min(T, sp.count - row0);
+      for (int t = 0; t < T; ++t) rows[t] = t < nrows ? a.list_in[row0 + t] : -1;
+      return nrows;
+    };
+    if (tid == 0) {
+      for (int k = 0; k < 2; ++k) {
+        const long item = blockIdx.x + (long)k * gridDim.x;
+        if (item < sp.items) {
+          const int nr = item_rows(item, s_rows[k]);
+          load_tile(a, ys + (size_t)k * T * RS, RS, s_rows[k], nr, 0, &bar[k]);
+        }
+      }
+    }
+    uint32_t phases = 0u;  // bit b = parity to wait for on buffer b
+    int k = 0;
+    for (long item = blockIdx.x; item < sp.items; item += gridDim.x, ++k) {
+      const int buf = k & 1;
+      const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
+      const int nrows = min(T, sp.count - tile * T);
+      const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
+      const uint32_t parity = (phases >> buf) & 1u;
+      if (tid == 0) s_fail = mbar_wait_bounded(&bar[buf], parity, a.err) ? 0 : 1;
+      __syncthreads();
+      if (s_fail) return;
+      mbar_try_wait(&bar[buf], parity);
+      phases ^= 1u << buf;
+      const float* yb = ys + (size_t)buf * T * RS;
+      uint32_t m = 0;
+      for (int g = gbeg + warp; g < gend; g += nwarps) {
+        float acc[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) acc[t] = 0.f;
+        accumulate_group<T, RSW, CONSTW>(acc, a.w, a.nq, yb, RS, g, 0, lane);
+        m |= epilogue_group<T>(acc, a, s_rows[buf], nrows, g, lane);
+      }
+      if (lane == 0 && m) atomicOr(&s_mask, m);
+      __syncthreads();  // every warp is done with this buffer and its rows
+      if (tid == 0) {
+        const uint32_t mm = s_mask;
+        s_mask = 0;
+        publish_rows<T>(a, mm, tile, sp.spl, s_rows[buf]);
+        const long next = item + 2L * gridDim.x;
+        if (next < sp.items) {
+          const int nr = item_rows(next, s_rows[buf]);
+          load_tile(a, ys + (size_t)buf * T * RS, RS, s_rows[buf], nr, 0, &bar[buf]);
+        }
+      }
+    }
+  } else if constexpr (KG == 1) {
+    // one buffer, whole rows (one chunk): reload per item, all groups of the part
+    uint32_t phase = 0;
+    int loaded_tile = -1;
+    for (long item = blockIdx.x; item < sp.items; item += gridDim.x) {
+      const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
+      const int row0 = tile * T;
+      const int nrows = min(T, sp.count - row0);
+      const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
+      __syncthreads();
+      if (tid < T) s_rows[0][tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
+      __syncthreads();
       if (tile != loaded_tile) {
         if (tid == 0) {
-          const uint32_t row_bytes = (uint32_t)a.Q * 4u;
-          mbar_expect_tx(&bar, row_bytes * (uint32_t)nrows);
-          for (int t = 0; t < nrows; ++t) {
-            const char* src = reinterpret_cast<const char*>(a.y_in + (size_t)s_rows[t] * a.N);
-            char* dst = reinterpret_cast<char*>(ys + (size_t)t * RS);
-            for (uint32_t off = 0; off < row_bytes; off += 32768u)
-              bulk_g2s(dst + off, src + off, min(32768u, row_bytes - off), &bar);
-          }
-          s_fail = mbar_wait_bounded(&bar, phase, a.err) ? 0 : 1;
+          load_tile(a, ys, RS, s_rows[0], nrows, 0, &bar[0]);
+          s_fail = mbar_wait_bounded(&bar[0], phase, a.err) ? 0 : 1;
         }
         __syncthreads();
         if (s_fail) return;
-        mbar_try_wait(&bar, phase);
+        mbar_try_wait(&bar[0], phase);
         phase ^= 1u;
         loaded_tile = tile;
       }
@@ -233,73 +359,61 @@ __global__ void __launch_bounds__(512) layer_kernel(const LayerArgs a) {
         float acc[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) acc[t] = 0.f;
-        accumulate_group<T, RSW, CONSTW>(acc, a, ys, RS, g, 0, lane);
-        m |= epilogue_group<T>(acc, a, s_rows, nrows, g, lane);
+        accumulate_group<T, RSW, CONSTW>(acc, a.w, a.nq, ys, RS, g, 0, lane);
+        m |= epilogue_group<T>(acc, a, s_rows[0], nrows, g, lane);
       }
       if (lane == 0 && m) atomicOr(&s_mask, m);
-    } else {
+      __syncthreads();
+      if (tid == 0) {
+        const uint32_t mm = s_mask;
+        s_mask = 0;
+        publish_rows<T>(a, mm, tile, sp.spl, s_rows[0]);
+      }
+    }
+  } else {
+    // input chunks (nq > 1): accumulators of KG groups per warp live across chunks
+    uint32_t phase = 0;
+    for (long item = blockIdx.x; item < sp.items; item += gridDim.x) {
+      const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
+      const int row0 = tile * T;
+      const int nrows = min(T, sp.count - row0);
+      const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
+      __syncthreads();
+      if (tid < T) s_rows[0][tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
+      __syncthreads();
       float acc[KG][T];
 #pragma unroll
-      for (int k = 0; k < KG; ++k)
+      for (int kk = 0; kk < KG; ++kk)
 #pragma unroll
-        for (int t = 0; t < T; ++t) acc[k][t] = 0.f;
+        for (int t = 0; t < T; ++t) acc[kk][t] = 0.f;
       for (int q = 0; q < a.nq; ++q) {
         if (q > 0) __syncthreads();
         if (tid == 0) {
-          const uint32_t row_bytes = (uint32_t)a.Q * 4u;
-          mbar_expect_tx(&bar, row_bytes * (uint32_t)nrows);
-          for (int t = 0; t < nrows; ++t) {
-            const char* src =
-                reinterpret_cast<const char*>(a.y_in + (size_t)s_rows[t] * a.N + (size_t)q * a.Q);
-            char* dst = reinterpret_cast<char*>(ys + (size_t)t * RS);
-            for (uint32_t off = 0; off < row_bytes; off += 32768u)
-              bulk_g2s(dst + off, src + off, min(32768u, row_bytes - off), &bar);
-          }
-          s_fail = mbar_wait_bounded(&bar, phase, a.err) ? 0 : 1;
+          load_tile(a, ys, RS, s_rows[0], nrows, q, &bar[0]);
+          s_fail = mbar_wait_bounded(&bar[0], phase, a.err) ? 0 : 1;
         }
         __syncthreads();
         if (s_fail) return;
-        mbar_try_wait(&bar, phase);
+        mbar_try_wait(&bar[0], phase);
         phase ^= 1u;
 #pragma unroll
-        for (int k = 0; k < KG; ++k) {
-          const int g = gbeg + warp + k * nwarps;
-          if (g < gend) accumulate_group<T, RSW, CONSTW>(acc[k], a, ys, RS, g, q, lane);
+        for (int kk = 0; kk < KG; ++kk) {
+          const int g = gbeg + warp + kk * nwarps;
+          if (g < gend) accumulate_group<T, RSW, CONSTW>(acc[kk], a.w, a.nq, ys, RS, g, q, lane);
         }
       }
-      loaded_tile = -1;
       uint32_t m = 0;
 #pragma unroll
-      for (int k = 0; k < KG; ++k) {
-        const int g = gbeg + warp + k * nwarps;
-        if (g < gend) m |= epilogue_group<T>(acc[k], a, s_rows, nrows, g, lane);
+      for (int kk = 0; kk < KG; ++kk) {
+        const int g = gbeg + warp + kk * nwarps;
+        if (g < gend) m |= epilogue_group<T>(acc[kk], a, s_rows[0], nrows, g, lane);
       }
       if (lane == 0 && m) atomicOr(&s_mask, m);
-    }
-
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t m = s_mask;
-      s_mask = 0;
-      if (a.epi != EPI_CENTROID) {
-        bool emit = true;
-        if (spl > 1) {
-          atomicOr(a.tile_mask + tile, m);
-          __threadfence();
-          const int tk = atomicAdd(a.tile_ticket + tile, 1);
-          emit = (tk == spl - 1);
-          if (emit) {
-            __threadfence();
-            m = atomicExch(a.tile_mask + tile, 0u);
-            a.tile_ticket[tile] = 0;
-          }
-        }
-        if (emit && m) {
-          const int base = atomicAdd(a.count_out, __popc(m));
-          int i = 0;
-          for (int t = 0; t < T; ++t)
-            if (m & (1u << t)) a.list_out[base + i++] = s_rows[t];
-        }
+      __syncthreads();
+      if (tid == 0) {
+        const uint32_t mm = s_mask;
+        s_mask = 0;
+        publish_rows<T>(a, mm, tile, sp.spl, s_rows[0]);
       }
     }
   }

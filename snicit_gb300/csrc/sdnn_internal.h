@@ -58,6 +58,11 @@ struct LayerArgs {
 // instances with row stride chunk + 32 of these chunk sizes read them as such.
 inline bool slot_index_in_bytes(int Q) { return Q == 1024 || Q == 4096; }
 __host__ __device__ constexpr bool rsw_in_bytes(int rsw) { return rsw == 1056 || rsw == 4128; }
+// Tile buffers of a layer-kernel instance (2 = load of the next tile overlaps
+// the current one); the dynamic shared memory is buffers * T * (chunk + 32) * 4.
+__host__ __device__ constexpr int layer_buffers(int kg, int rsw) {
+  return (kg == 1 && rsw_in_bytes(rsw)) ? 2 : 1;
+}
 
 // Kernel instance selection.
 struct LayerKernelKey {
@@ -98,6 +103,21 @@ struct Layer0Args {
 bool layer0_bits_supported(int N);
 int layer0_bits_grid(int N, int num_sms, int threads);
 cudaError_t launch_layer0_bits(const Layer0Args& a, int grid, int threads, cudaStream_t s);
+
+// Post-threshold layers with no residue rows left (post_chain.cu): one
+// cluster carries the K centroid rows through layers [first, last).
+struct ChainArgs {
+  const LayerDev* layers;    // [L] device table
+  int32_t first, last;
+  const float* y_in;         // activations at the threshold
+  float* y_out;              // final buffer (centroid rows written after `last`)
+  const int32_t* clist;
+  const int32_t* ccount;
+  int32_t N, G;
+  float clampv;
+};
+int chain_capacity(int N);  // largest centroid count the chain kernel takes (0 = none)
+cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);

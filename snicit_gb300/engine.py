@@ -21,7 +21,8 @@ class Engine:
 
     def __init__(self, num_neurons=1024, num_layers=120, mode="SNICIT", threshold=30,
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
-                 device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True):
+                 device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
+                 chain=True):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -38,7 +39,8 @@ class Engine:
         cfg.tile_rows = int(tile_rows)
         cfg.threads = int(threads)
         cfg.flags = ((0 if binary_first_layer else _lib.FLAG_NO_BINARY_FIRST_LAYER)
-                     | (0 if placement else _lib.FLAG_NO_PLACEMENT))
+                     | (0 if placement else _lib.FLAG_NO_PLACEMENT)
+                     | (0 if chain else _lib.FLAG_NO_CHAIN))
         self.cfg = cfg
         self.N = cfg.num_neurons
         self.L = cfg.num_layers
