@@ -341,11 +341,108 @@ def run_ours(args):
             "gpu_launches": st["launches"] * args.steps,
             "clocks": clk.summary(),
         }
+        if not args.no_serve:
+            line["serving"] = run_serving(args, sg, local)
         print(json.dumps(line), flush=True)
     eng.close()
     plain.close()
     if dist:
         dist.destroy_process_group()
+
+
+def _percentile(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
+
+
+def serve_stream(sg, eng, head_w, head_b, pool, arrivals, sizes, offsets, **server_kw):
+    """Replays a request stream against a Server; returns (latencies s, rows, wall s, stats)."""
+    with sg.Server(eng, head_w, head_b, **server_kw) as sv:
+        sv.wait(sv.submit(pool[:64]))  # first pass: graph capture, not part of the stream
+        ids = [None] * len(sizes)
+
+        def submitter():
+            t0 = time.perf_counter()
+            for i, (a, n, o) in enumerate(zip(arrivals, sizes, offsets)):
+                d = t0 + a - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                ids[i] = sv.submit(pool[o:o + n])
+
+        t_start = time.perf_counter()
+        th = threading.Thread(target=submitter)
+        th.start()
+        lat = []
+        for i in range(len(sizes)):
+            while ids[i] is None:
+                time.sleep(1e-4)
+            lat.append(sv.wait(ids[i]).latency_s)
+        wall = time.perf_counter() - t_start
+        th.join()
+        st = sv.stats()
+    return lat, int(sum(sizes)), wall, st
+
+
+def run_serving(args, sg, local=0):
+    """Serving loop on the sparse MLP (1024 inputs, 120 layers of width 1024 at
+    3% density, N(0, 0.3^2) weights, bias -0.05, clamp 32, dense 1024x10 head):
+    a seeded Poisson stream of requests (sizes log-uniform in [1, 4096]) at
+    --serve-rate req/s, replayed in real time against the continuous-batching
+    server (SNICIT mode, clustering across co-resident requests, and SNIG
+    mode), against the per-request path (one request per pass, SNIG), and at
+    saturation (all requests queued at once)."""
+    import numpy as np
+    N, L = 1024, 120
+    layers, hw, hb = sg.sparse_mlp(SEED, N=N, L=L)
+    arrivals, sizes = sg.request_stream(SEED, args.serve_requests, rate=args.serve_rate)
+    pool = sg.mlp_inputs(SEED, 0, 16384, N)
+    rng = np.random.default_rng([SEED, 5])
+    offsets = [int(rng.integers(0, len(pool) - n + 1)) for n in sizes]
+    out = {"workload": f"serve-mlp-{N}x{L}", "requests": len(sizes), "rate_req_s": args.serve_rate,
+           "rows": int(sizes.sum()), "mean_rows": float(sizes.mean()),
+           "arrival_span_s": float(arrivals[-1])}
+    engines = {}
+    for mode in ("SNICIT", "SNIG"):
+        e = sg.Engine(N, L, mode=mode, threshold=30, batch=4096, bias=-0.05, num_centroids=50,
+                      device=local)
+        for l, (ro, c, v) in enumerate(layers):
+            e.set_layer_csr(l, ro, c, v)
+        engines[mode] = e
+    arms = [("continuous_snicit", "SNICIT", dict(slots=2), arrivals),
+            ("continuous_plain", "SNIG", dict(slots=2), arrivals),
+            ("per_request_plain", "SNIG", dict(slots=1, max_requests_per_pass=1), arrivals),
+            ("saturation_snicit", "SNICIT", dict(slots=2), np.zeros_like(arrivals)),
+            ("saturation_plain", "SNIG", dict(slots=2), np.zeros_like(arrivals))]
+    for name, mode, kw, arr in arms:
+        lat, rows, wall, st = serve_stream(sg, engines[mode], hw, hb, pool, arr, sizes, offsets,
+                                           max_rows=16384, **kw)
+        out[name] = {"samples_per_s": rows / wall, "p50_ms": _percentile(lat, 0.5) * 1e3,
+                     "p99_ms": _percentile(lat, 0.99) * 1e3, "passes": st["passes"],
+                     "max_rows_in_pass": st["max_rows_in_pass"], "wall_s": wall}
+    for e in engines.values():
+        e.close()
+    return out
+
+
+CASES = {
+    # name: (N, L, rows, mode, threshold) -- small fixed cases for ncu captures
+    "plain-n4096": (4096, 6, 8192, "SNIG", 6),
+    "chain-n4096": (4096, 60, 4096, "SNICIT", 30),
+}
+
+
+def run_case(args):
+    """One small engine run (two inferences) for profiling; prints its stats."""
+    import snicit_gb300 as sg
+    N, L, B, mode, t = CASES[args.case]
+    Y0 = sg.generate_inputs(N, SEED, 0, B)
+    eng = sg.Engine(N, L, mode=mode, threshold=t, batch=B, bias=sg.load().sdnn_reference_bias(N),
+                    num_centroids=args.centroids, tile_rows=args.tile, threads=args.threads)
+    eng.generate_weights(SEED, NNZ, 0.0625)
+    for _ in range(2):
+        eng.infer(Y0)
+    print(json.dumps({"case": args.case, "stats": eng.stats()}), flush=True)
+    eng.close()
 
 
 def main():
@@ -363,8 +460,19 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serve-only", action="store_true", help="only the serving-loop measurement")
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--case", default=None, choices=sorted(CASES),
+                    help="run a small fixed case (used for ncu captures) instead of the bench")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.serve_only:
+        import snicit_gb300 as sg
+        print(json.dumps({"serving": run_serving(args, sg)}), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -174,6 +174,19 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows,
 int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
                       int32_t* d_flags, void* stream);
 
+/* Several input batches of uneven size in one launch schedule: their rows are
+ * gathered back to back and run as one inference (rows are independent, so
+ * each batch gets its own category set; in SNICIT mode the clustering spans
+ * all batches).  inputs[b] has rows[b] x N floats, flags[b] (optional)
+ * receives rows[b] ints.  The total must not exceed cfg.batch.  Replaces the
+ * reference's per-batch offset loop (src/SDGC/SNICIT/SNICIT.hpp:121-202) where
+ * each batch is a separate inference. */
+int sdnn_infer_batches_host(sdnn_engine* e, const float* const* inputs, const int64_t* rows,
+                            int32_t num_batches, int32_t* const* flags);
+/* Device-pointer variant (inputs and flags in device memory, 16-byte aligned). */
+int sdnn_infer_batches_device(sdnn_engine* e, const float* const* d_inputs, const int64_t* rows,
+                              int32_t num_batches, int32_t* const* d_flags, void* stream);
+
 /* Inputs read from a reference-format TSV ("sample<TAB>feature<TAB>value",
  * 1-based), rows [row_offset, row_offset + rows) into a host buffer
  * (src/SDGC/utility.hpp:160-191,268-293). */
@@ -214,6 +227,58 @@ int sdnn_layer_noalloc(sdnn_engine* e, int32_t layer, const float* d_y_in, float
  * on the given sample rows (host buffer) and appends one JSON line per tried
  * setting to record_path (if not NULL).  Applies the fastest setting. */
 int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows, const char* record_path);
+
+/* ---- serving: continuous batching of requests ---------------------------- */
+
+typedef struct sdnn_server sdnn_server;
+
+typedef struct sdnn_server_config {
+  int32_t slots;           /* passes in flight: one engine, stream and worker each */
+  int32_t head_outputs;    /* width of the dense head after the last layer (0 = none) */
+  int64_t max_rows;        /* upper bound of rows per pass (0 = none; default 16384) */
+  double memory_fraction;  /* share of free device memory the slots may take: the
+                              rows per pass are what fits in it (default 0.25)     */
+  int64_t max_pending;     /* queued requests before sdnn_submit answers BUSY       */
+  int64_t max_delay_us;    /* batching window: a pass that is not full waits until
+                              its oldest request has queued this long (default 0) */
+  int32_t max_requests_per_pass; /* 0 = as many as fit; 1 = one request per pass
+                                    (the per-request path, for comparison)        */
+  int32_t reserved[5];
+} sdnn_server_config;
+
+typedef struct sdnn_server_stats {
+  int64_t passes, rows, requests, max_rows_in_pass, queued, slot_rows;
+  int32_t slots;
+  int32_t reserved[7];
+} sdnn_server_stats;
+
+int sdnn_server_config_default(sdnn_server_config* cfg);
+
+/* A request server over the network of `model` (an engine with its weights
+ * set; the server copies them into its own slot engines).  head_w is N x
+ * head_outputs (row-major, by neuron), head_b has head_outputs entries: the
+ * dense output layer of the beyond nets (src/beyond/general.hpp:74-102).
+ * Requests arrive with sdnn_submit at any time and are admitted, in arrival
+ * order, into the first free slot while they fit its row capacity; slots run
+ * concurrently.  The reference has no serving loop; its beyond driver runs
+ * fixed rounds (src/beyond/SNICIT/SNICIT.hpp:494-641). */
+int sdnn_server_create(sdnn_engine* model, const sdnn_server_config* cfg, const float* head_w,
+                       const float* head_b, sdnn_server** out);
+int sdnn_server_destroy(sdnn_server* sv);
+/* Rows a slot holds (the largest admissible request). */
+int64_t sdnn_server_capacity(const sdnn_server* sv);
+/* Queues `rows` x N host floats (copied); SDNN_ERR_BUSY when the queue is full,
+ * SDNN_ERR_INVALID when rows exceed the slot capacity. */
+int sdnn_submit(sdnn_server* sv, const float* rows_host, int64_t rows, uint64_t* request_id);
+/* done = 1 when finished, then copies flags (rows), logits (rows x head),
+ * argmax (rows) and the submit-to-completion latency in seconds (each
+ * optional) and forgets the request. */
+int sdnn_poll(sdnn_server* sv, uint64_t id, int32_t* done, int32_t* flags, float* logits,
+              int32_t* argmax, double* latency_s);
+/* Blocks until the request is finished; same outputs as sdnn_poll. */
+int sdnn_wait(sdnn_server* sv, uint64_t id, int32_t* flags, float* logits, int32_t* argmax,
+              double* latency_s);
+int sdnn_server_get_stats(sdnn_server* sv, sdnn_server_stats* out);
 
 /* ---- synthetic data and reference file formats --------------------------- */
 

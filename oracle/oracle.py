@@ -125,3 +125,10 @@ def ref_candidates(Ylive, sample=32):
     n = lib().oracle_ref_candidates(_p(Ylive), Ylive.shape[0], Ylive.shape[1], int(sample),
                                     _p(out))
     return out[:n].copy()
+
+
+def head(Y, head_w, head_b):
+    """Dense output head in FP64: logits = Y . W + b, no activation
+    (dense_output, src/beyond/general.hpp:74-102); argmax = first maximum."""
+    logits = np.asarray(Y, np.float64) @ np.asarray(head_w, np.float64) + np.asarray(head_b, np.float64)
+    return logits, np.argmax(logits, axis=1).astype(np.int32)

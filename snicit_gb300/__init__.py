@@ -8,3 +8,4 @@ from .engine import (Engine, coo_to_csr, generate_inputs, generate_layer_coo,  #
                      generate_layer_csr, read_inputs_tsv, write_categories_tsv,
                      write_inputs_tsv)
 from .sdgc import BF, SNICIT, SNIG, XY  # noqa: F401
+from .serving import Server, mlp_inputs, request_stream, sparse_mlp  # noqa: F401

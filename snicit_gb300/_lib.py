@@ -51,6 +51,24 @@ class Stats(ctypes.Structure):
     ]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("slots", ctypes.c_int32), ("head_outputs", ctypes.c_int32),
+        ("max_rows", ctypes.c_int64), ("memory_fraction", ctypes.c_double),
+        ("max_pending", ctypes.c_int64), ("max_delay_us", ctypes.c_int64),
+        ("max_requests_per_pass", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("passes", ctypes.c_int64), ("rows", ctypes.c_int64), ("requests", ctypes.c_int64),
+        ("max_rows_in_pass", ctypes.c_int64), ("queued", ctypes.c_int64),
+        ("slot_rows", ctypes.c_int64), ("slots", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
+    ]
+
+
 # (name, restype, argtypes) of every exported entry point
 P, I32, I64, U64, F32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_float
 SIGNATURES = [
@@ -68,12 +86,22 @@ SIGNATURES = [
     ("sdnn_finalize_weights", ctypes.c_int, [P]),
     ("sdnn_infer_host", ctypes.c_int, [P, P, I64, P, P, P]),
     ("sdnn_infer_device", ctypes.c_int, [P, P, I64, P, P]),
+    ("sdnn_infer_batches_host", ctypes.c_int, [P, P, P, I32, P]),
+    ("sdnn_infer_batches_device", ctypes.c_int, [P, P, P, I32, P, P]),
     ("sdnn_read_inputs_tsv", ctypes.c_int, [ctypes.c_char_p, I32, I64, I64, P]),
     ("sdnn_read_activations", ctypes.c_int, [P, P, I64]),
     ("sdnn_get_stats", ctypes.c_int, [P, P]),
     ("sdnn_get_layer_rows", ctypes.c_int, [P, P, I32]),
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_layer_noalloc", ctypes.c_int, [P, I32, P, P, I64, P, P]),
+    ("sdnn_server_config_default", ctypes.c_int, [P]),
+    ("sdnn_server_create", ctypes.c_int, [P, P, P, P, P]),
+    ("sdnn_server_destroy", ctypes.c_int, [P]),
+    ("sdnn_server_capacity", I64, [P]),
+    ("sdnn_submit", ctypes.c_int, [P, P, I64, P]),
+    ("sdnn_poll", ctypes.c_int, [P, U64, P, P, P, P, P]),
+    ("sdnn_wait", ctypes.c_int, [P, U64, P, P, P, P]),
+    ("sdnn_server_get_stats", ctypes.c_int, [P, P]),
     ("sdnn_generate_inputs", ctypes.c_int, [I32, U64, I64, I64, P]),
     ("sdnn_generate_layer_coo", ctypes.c_int, [I32, U64, I32, I32, F32, P, P, P]),
     ("sdnn_write_weights_tsv", ctypes.c_int, [P, ctypes.c_char_p]),

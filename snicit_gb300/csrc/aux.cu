@@ -29,6 +29,48 @@ void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s) {
   iota_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, count, n);
 }
 
+// Rows of the current inference come from a device scalar (set just before a
+// captured graph is launched), so one graph serves every row count.
+__global__ void set_scalar_kernel(int32_t* p, int32_t v) { *p = v; }
+void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s) { set_scalar_kernel<<<1, 1, 0, s>>>(p, v); }
+
+__global__ void begin_rows_kernel(const int32_t* nrows, int32_t* list, int32_t* count,
+                                  int32_t* zero_a, int32_t* zero_b) {
+  const int n = *nrows;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    list[i] = i;
+    if (zero_a) zero_a[i] = 0;
+    if (zero_b) zero_b[i] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
+}
+void launch_begin_rows(const int32_t* nrows, int32_t* list, int32_t* count, int32_t* zero_a,
+                       int32_t* zero_b, cudaStream_t s) {
+  begin_rows_kernel<<<264, 256, 0, s>>>(nrows, list, count, zero_a, zero_b);
+}
+
+__global__ void zero_rows_kernel(const int32_t* nrows, int32_t* a, int32_t* b) {
+  const int n = *nrows;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    a[i] = 0;
+    if (b) b[i] = 0;
+  }
+}
+void launch_zero_rows(const int32_t* nrows, int32_t* a, int32_t* b, cudaStream_t s) {
+  zero_rows_kernel<<<264, 256, 0, s>>>(nrows, a, b);
+}
+
+__global__ void copy_rows_kernel(const int32_t* nrows, const float4* src, float4* dst, int32_t n4) {
+  const size_t total = (size_t)(*nrows) * (size_t)n4;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+void launch_copy_rows(const int32_t* nrows, const float* src, float* dst, int32_t N, cudaStream_t s) {
+  copy_rows_kernel<<<1024, 256, 0, s>>>(nrows, reinterpret_cast<const float4*>(src),
+                                        reinterpret_cast<float4*>(dst), N / 4);
+}
+
 __global__ void mark_rows_kernel(const int32_t* list, const int32_t* count, int32_t* flags,
                                  int32_t value) {
   const int n = *count;
@@ -372,6 +414,84 @@ void launch_materialize(const float* y, const int32_t* state, const int32_t* csl
                         const int32_t* perm, int32_t N, float* out, int32_t rows, cudaStream_t s) {
   materialize_kernel<<<grid_for(rows, 1, 8192), 256, 0, s>>>(y, state, cslot, clist, is_centroid,
                                                              res_flag, perm, N, rows, out);
+}
+
+// Dense output head on the final activations (dense_output,
+// src/beyond/general.hpp:74-102: logits = y . H + b, no activation), one warp
+// per row, rows read the way materialize_kernel reads them (dead rows are
+// zero, SNICIT rows are recovered).  Hp is the head stored by final position
+// (Hp[p][k] = H[neuron at p][k]); lane-strided sums over positions, then a
+// fixed xor-shuffle tree: deterministic.  argmax: first maximal logit.
+template <int H>
+__global__ void head_kernel(const float* __restrict__ y, const int32_t* state, const int32_t* cslot,
+                            const int32_t* clist, const int32_t* is_centroid,
+                            const int32_t* res_flag, const float* __restrict__ Hp,
+                            const float* __restrict__ hb, int32_t N, int32_t rows, float* logits,
+                            int32_t* argmax) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int r = wid; r < rows; r += nw) {
+    float acc[H];
+#pragma unroll
+    for (int k = 0; k < H; ++k) acc[k] = 0.f;
+    const int st = state[r];
+    if (st != 0) {
+      const float* yr = y + (size_t)r * N;
+      const bool plain = st == 1 || is_centroid[r];
+      const float* yc = plain ? yr : y + (size_t)clist[cslot[r]] * N;
+      const bool has_res = !plain && res_flag[r];
+      for (int p = lane; p < N; p += 32) {
+        const float v = plain ? yr[p] : (has_res ? yr[p] + yc[p] : yc[p]);
+        if (v != 0.f) {
+#pragma unroll
+          for (int k = 0; k < H; ++k) acc[k] = fmaf(v, __ldg(Hp + (size_t)p * H + k), acc[k]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < H; ++k) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    }
+    if (lane == 0) {
+      int best = 0;
+      float bv = 0.f;
+#pragma unroll
+      for (int k = 0; k < H; ++k) {
+        const float v = acc[k] + hb[k];
+        logits[(size_t)r * H + k] = v;
+        if (k == 0 || v > bv) {
+          bv = v;
+          best = k;
+        }
+      }
+      argmax[r] = best;
+    }
+  }
+}
+
+bool launch_head(const float* y, const int32_t* state, const int32_t* cslot, const int32_t* clist,
+                 const int32_t* is_centroid, const int32_t* res_flag, const float* Hp,
+                 const float* hb, int32_t H, int32_t N, int32_t rows, float* logits,
+                 int32_t* argmax, cudaStream_t s) {
+  const int grid = grid_for(rows, 8, 2048);
+#define SDNN_HEAD(K)                                                                           \
+  case K:                                                                                     \
+    head_kernel<K><<<grid, 256, 0, s>>>(y, state, cslot, clist, is_centroid, res_flag, Hp, hb, N, \
+                                        rows, logits, argmax);                                \
+    return true;
+  switch (H) {
+    SDNN_HEAD(1)
+    SDNN_HEAD(2)
+    SDNN_HEAD(4)
+    SDNN_HEAD(8)
+    SDNN_HEAD(10)
+    SDNN_HEAD(16)
+    SDNN_HEAD(32)
+    default: return false;
+  }
+#undef SDNN_HEAD
 }
 
 }  // namespace sdnn

@@ -121,6 +121,7 @@ struct sdnn_engine {
   int32_t* d_ids = nullptr;
   int32_t* d_idcount = nullptr;
   float* d_in = nullptr;
+  int32_t* d_rows = nullptr;      // row count of the current inference
   int32_t* d_fallback = nullptr;  // layer-0 rows of non-binary tiles
   int32_t* d_fbcount = nullptr;
   int bits_grid = 0;
@@ -207,6 +208,7 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_in);
   dfree(e->d_fallback);
   dfree(e->d_fbcount);
+  dfree(e->d_rows);
   if (e->h_counts) cudaFreeHost(e->h_counts);
   e->h_counts = nullptr;
   e->cap = 0;
@@ -327,6 +329,7 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
   T(A(&e->d_fbcount, 16));
+  T(A(&e->d_rows, 16));
   if (rc == cudaSuccess) T(cudaMallocHost((void**)&e->h_counts, 16));
   if (rc != cudaSuccess) {
     free_buffers(e);
@@ -631,26 +634,27 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
             bool capturing) {
   const int L = e->L;
   const int T = effective_threshold(e);
-  const size_t N = (size_t)e->N;
   const cudaStream_t s = e->stream;
   int rc;
   float* ybuf = e->d_y[(T - 1 + 2) & 1];  // activations at the threshold
   const int32_t* live = e->d_list[T & 1];
   const int32_t* live_count = e->d_counts + T;
+  (void)rows;  // the row count is read on the device from d_rows
   if (phase == PH_ALL || phase == PH_PRE) {
     if ((rc = record(e, 0, capturing))) return rc;
     CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
-    CK(cudaMemsetAsync(d_flags, 0, (size_t)rows * 4, s));
-    CK(cudaMemsetAsync(e->d_state, 0, (size_t)rows * 4, s));
-    launch_iota(e->d_list[0], e->d_counts, (int32_t)rows, s);
+    launch_begin_rows(e->d_rows, e->d_list[0], e->d_counts, d_flags, e->d_state, s);
     e->launches++;
     if ((rc = enqueue_plain_layers(e, rows, d_in, T, capturing))) return rc;
   }
   if (phase == PH_PRE) {
-    if (T == 0) CK(cudaMemcpyAsync(ybuf, d_in, (size_t)rows * N * 4, cudaMemcpyDeviceToDevice, s));
+    if (T == 0) {
+      launch_copy_rows(e->d_rows, d_in, ybuf, e->N, s);
+      e->launches++;
+    }
     CK(cudaMemsetAsync(e->d_rcounts, 0, (size_t)(L + 4) * 4, s));
-    CK(cudaMemsetAsync(e->d_iscent, 0, (size_t)rows * 4, s));
-    CK(cudaMemsetAsync(e->d_resflag, 0, (size_t)rows * 4, s));
+    launch_zero_rows(e->d_rows, e->d_iscent, e->d_resflag, s);
+    e->launches++;
     CK(cudaMemsetAsync(e->d_ccount, 0, 16, s));
     CK(cudaMemsetAsync(e->d_ncand, 0, 16, s));
     ClusterArgs c{};
@@ -740,7 +744,7 @@ int run_phase(sdnn_engine* e, int slot, int phase, int64_t rows, const float* d_
     return rc;
   }
   GraphSlot& g = e->graphs[slot];
-  const GraphKey key{rows, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
+  const GraphKey key{0, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
                      e->key.T, e->threads, phase == PH_POST_CHAIN ? e->chain_kc : 0};
   if (!g.exec || !(g.key == key)) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -777,6 +781,9 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   e->last_T = T;
   e->last_rows = rows;
   e->run_launches = 0;
+  // the graphs read the row count from d_rows (one graph for every count)
+  launch_set_scalar(e->d_rows, (int32_t)rows, e->stream);
+  e->run_launches++;
   int rc;
   if (e->cfg.mode != SDNN_MODE_SNICIT || T >= e->L) {
     if ((rc = run_phase(e, 0, PH_ALL, rows, d_in, d_flags))) return rc;
@@ -1114,6 +1121,92 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows, int32_t* flag
   return SDNN_OK;
 }
 
+int sdnn_infer_batches_host(sdnn_engine* e, const float* const* inputs, const int64_t* rows,
+                            int32_t num_batches, int32_t* const* flags) {
+  if (!e || !inputs || !rows || num_batches <= 0) return SDNN_ERR_INVALID;
+  int64_t total = 0;
+  for (int32_t b = 0; b < num_batches; ++b) {
+    if (rows[b] < 0 || (rows[b] > 0 && !inputs[b])) return fail(e, SDNN_ERR_INVALID, "bad batch");
+    total += rows[b];
+  }
+  if (total <= 0) return fail(e, SDNN_ERR_INVALID, "no rows");
+  if (total > e->cfg.batch)
+    return fail(e, SDNN_ERR_INVALID, "batches exceed the engine's batch capacity");
+  int rc = prepare(e, total);
+  if (rc) return rc;
+  const int64_t N = e->N;
+  // gather the batches back to back into the engine's input rows
+  int64_t off = 0;
+  for (int32_t b = 0; b < num_batches; ++b) {
+    if (rows[b] > 0)
+      CK(cudaMemcpyAsync(e->d_in + off * N, inputs[b], (size_t)(rows[b] * N) * 4,
+                         cudaMemcpyHostToDevice, e->stream));
+    off += rows[b];
+  }
+  rc = run(e, total, e->d_in, e->d_flags);
+  if (rc) return rc;
+  off = 0;
+  for (int32_t b = 0; b < num_batches; ++b) {
+    if (flags && flags[b] && rows[b] > 0)
+      CK(cudaMemcpyAsync(flags[b], e->d_flags + off, (size_t)rows[b] * 4, cudaMemcpyDeviceToHost,
+                         e->stream));
+    off += rows[b];
+  }
+  rc = check_device_error(e);
+  if (rc) return rc;
+  return collect_stats(e);
+}
+
+int sdnn_infer_batches_device(sdnn_engine* e, const float* const* d_inputs, const int64_t* rows,
+                              int32_t num_batches, int32_t* const* d_flags, void* stream) {
+  if (!e || !d_inputs || !rows || !d_flags || num_batches <= 0) return SDNN_ERR_INVALID;
+  int64_t total = 0;
+  for (int32_t b = 0; b < num_batches; ++b) {
+    if (rows[b] < 0 || (rows[b] > 0 && (!d_inputs[b] || !d_flags[b])))
+      return fail(e, SDNN_ERR_INVALID, "bad batch");
+    total += rows[b];
+  }
+  if (total <= 0) return fail(e, SDNN_ERR_INVALID, "no rows");
+  int rc = prepare(e, total);
+  if (rc) return rc;
+  cudaStream_t user = (cudaStream_t)stream;
+  cudaEvent_t joined = nullptr;
+  if (user && user != e->stream) {
+    CK(cudaEventCreateWithFlags(&joined, cudaEventDisableTiming));
+    CK(cudaEventRecord(joined, user));
+    CK(cudaStreamWaitEvent(e->stream, joined, 0));
+  }
+  const int64_t N = e->N;
+  int64_t off = 0;
+  for (int32_t b = 0; b < num_batches; ++b) {
+    if (rows[b] > 0)
+      CK(cudaMemcpyAsync(e->d_in + off * N, d_inputs[b], (size_t)(rows[b] * N) * 4,
+                         cudaMemcpyDeviceToDevice, e->stream));
+    off += rows[b];
+  }
+  rc = run(e, total, e->d_in, e->d_flags);
+  if (rc == SDNN_OK) {
+    off = 0;
+    for (int32_t b = 0; b < num_batches; ++b) {
+      if (rows[b] > 0) {
+        const cudaError_t ce = cudaMemcpyAsync(d_flags[b], e->d_flags + off, (size_t)rows[b] * 4,
+                                               cudaMemcpyDeviceToDevice, e->stream);
+        if (ce != cudaSuccess) {
+          rc = cuda_fail(e, ce, "cudaMemcpyAsync");
+          break;
+        }
+      }
+      off += rows[b];
+    }
+  }
+  if (joined) {
+    cudaEventRecord(joined, e->stream);
+    cudaStreamWaitEvent(user, joined, 0);
+    cudaEventDestroy(joined);
+  }
+  return rc;
+}
+
 int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows) {
   if (!e || !out) return SDNN_ERR_INVALID;
   if (!e->have_run) return fail(e, SDNN_ERR_STATE, "no inference has run");
@@ -1237,5 +1330,28 @@ int engine_layer_setup(sdnn_engine* e, int layer, LayerArgs* a, LayerKernelKey* 
   return SDNN_OK;
 }
 cudaStream_t engine_stream(const sdnn_engine* e) { return e->stream; }
+
+// ---- hooks for the serving loop (serve.cpp)
+void engine_copy_weights(sdnn_engine* dst, const sdnn_engine* src) {
+  dst->gen = src->gen;
+  dst->hw = src->hw;
+  dst->hbias = src->hbias;
+  dst->weights_dirty = true;
+}
+int engine_prepare(sdnn_engine* e, int64_t rows) { return prepare(e, rows); }
+float* engine_input(sdnn_engine* e) { return e->d_in; }
+int32_t* engine_flags(sdnn_engine* e) { return e->d_flags; }
+int engine_run(sdnn_engine* e, int64_t rows) { return run(e, rows, e->d_in, e->d_flags); }
+int engine_check(sdnn_engine* e) { return check_device_error(e); }
+// Positions of the neurons after the last layer (empty = identity).
+std::vector<int32_t> engine_final_positions(const sdnn_engine* e) {
+  return e->pos.empty() ? std::vector<int32_t>() : e->pos[e->L - 1];
+}
+bool engine_head(sdnn_engine* e, const float* Hp, const float* hb, int32_t H, int64_t rows,
+                 float* logits, int32_t* argmax) {
+  return launch_head(e->d_y[(e->L - 1) & 1], e->d_state, e->d_cslot, e->d_clist, e->d_iscent,
+                     e->d_resflag, Hp, hb, H, e->N, (int32_t)rows, logits, argmax, e->stream);
+}
+std::string engine_error(const sdnn_engine* e) { return e->err; }
 void engine_set_error(sdnn_engine* e, const std::string& msg) { e->err = msg; }
 }  // namespace sdnn

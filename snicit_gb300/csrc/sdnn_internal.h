@@ -121,6 +121,12 @@ cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);
+void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s);
+// list[i] = i and zero_a[i] = zero_b[i] = 0 for i < *nrows; *count = *nrows
+void launch_begin_rows(const int32_t* nrows, int32_t* list, int32_t* count, int32_t* zero_a,
+                       int32_t* zero_b, cudaStream_t s);
+void launch_zero_rows(const int32_t* nrows, int32_t* a, int32_t* b, cudaStream_t s);
+void launch_copy_rows(const int32_t* nrows, const float* src, float* dst, int32_t N, cudaStream_t s);
 void launch_identify(const float* y, const int32_t* list, const int32_t* count, int32_t N,
                      int32_t* flags, cudaStream_t s);
 void launch_flags_to_ids(const int32_t* flags, int32_t n, int32_t* ids, int32_t* count,
@@ -161,5 +167,13 @@ void launch_recover(const float* y, const int32_t* live, const int32_t* live_cou
 void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
                         const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
                         const int32_t* perm, int32_t N, float* out, int32_t rows, cudaStream_t s);
+
+// Dense output head (logits = recovered final row . H + b) for H in
+// {1, 2, 4, 8, 10, 16, 32}; Hp is stored by final position.  False if H is
+// not one of those.
+bool launch_head(const float* y, const int32_t* state, const int32_t* cslot, const int32_t* clist,
+                 const int32_t* is_centroid, const int32_t* res_flag, const float* Hp,
+                 const float* hb, int32_t H, int32_t N, int32_t rows, float* logits,
+                 int32_t* argmax, cudaStream_t s);
 
 }  // namespace sdnn

@@ -117,6 +117,25 @@ class Engine:
                                           ctypes.c_void_p(int(flags_ptr)),
                                           ctypes.c_void_p(int(stream_ptr)) if stream_ptr else None))
 
+    def infer_batches(self, batches):
+        """Host batches (list of rows x N arrays) in one launch schedule; returns flags per batch."""
+        arrs = [np.ascontiguousarray(b, dtype=np.float32) for b in batches]
+        nb = len(arrs)
+        ptrs = (ctypes.c_void_p * nb)(*[a.ctypes.data for a in arrs])
+        rows = (ctypes.c_int64 * nb)(*[a.shape[0] for a in arrs])
+        outs = [np.zeros(a.shape[0], dtype=np.int32) for a in arrs]
+        fptrs = (ctypes.c_void_p * nb)(*[o.ctypes.data for o in outs])
+        self._ck(load().sdnn_infer_batches_host(self._h, ptrs, rows, nb, fptrs))
+        return outs
+
+    def infer_batches_device(self, in_ptrs, rows, flag_ptrs, stream_ptr=None):
+        nb = len(in_ptrs)
+        p = (ctypes.c_void_p * nb)(*[int(x) for x in in_ptrs])
+        r = (ctypes.c_int64 * nb)(*[int(x) for x in rows])
+        f = (ctypes.c_void_p * nb)(*[int(x) for x in flag_ptrs])
+        self._ck(load().sdnn_infer_batches_device(
+            self._h, p, r, nb, f, ctypes.c_void_p(int(stream_ptr)) if stream_ptr else None))
+
     def activations(self, rows):
         out = np.zeros((rows, self.N), dtype=np.float32)
         self._ck(load().sdnn_read_activations(self._h, _ptr(out), int(rows)))

@@ -320,3 +320,21 @@ def test_chain_path_is_bitwise_equal_to_per_layer_path(N, L, B, T, K):
     assert np.array_equal(out[True][4], out[False][4])
     Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
     _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"chain N={N}", Y32=Y32)
+
+
+@pytest.mark.parametrize("mode", ["SNIG", "SNICIT"])
+def test_uneven_batches_in_one_schedule(mode):
+    """Uneven batches run as one schedule give each batch its own category set
+    (the same as running it alone), and graphs are reused across row counts."""
+    N, L, seed = 1024, 40, 91
+    sizes = [500, 37, 1200, 1, 260]
+    batches = [sg.generate_inputs(N, seed, 10000 * i, n) for i, n in enumerate(sizes)]
+    layers = _layers(N, L, seed)
+    with sg.Engine(N, L, mode=mode, threshold=12, batch=sum(sizes), bias=-0.3) as eng:
+        eng.generate_weights(seed)
+        flags = eng.infer_batches(batches)
+        flags2 = eng.infer_batches(batches[::-1])[::-1]
+        alone = [eng.infer(b)[0] for b in batches]
+    for f, f2, a, b in zip(flags, flags2, alone, batches):
+        _, alive, _ = orc.infer(layers, N, -0.3, b, precision=64, want_y=False)
+        assert np.array_equal(f, alive) and np.array_equal(f2, alive) and np.array_equal(a, alive)
