@@ -75,7 +75,10 @@ typedef struct sdnn_config {
   int32_t tile_rows;     /* rows per CTA in the layer kernel (0 = automatic)      */
   int32_t threads;       /* threads per CTA in the layer kernel (0 = automatic)   */
   int32_t flags;         /* SDNN_FLAG_* bits (0 = all optimisations on)            */
-  int32_t reserved[4];
+  int32_t merge_start;   /* SNICIT: first plain layer after which identical rows
+                            are merged (0 = automatic)                            */
+  int32_t merge_every;   /* ... and then after every merge_every-th layer (0 = 1)  */
+  int32_t reserved[2];
 } sdnn_config;
 
 /* sdnn_config.flags: switch off layout optimisations (results are identical
@@ -84,6 +87,10 @@ typedef struct sdnn_config {
 #define SDNN_FLAG_NO_PLACEMENT 2           /* keep neuron order; no degree/bank placement   */
 #define SDNN_FLAG_NO_CHAIN 4               /* SNICIT: per-layer post launches even when no  */
                                            /* residue row is left                           */
+#define SDNN_FLAG_NO_MERGE 8               /* SNICIT: no merging of bitwise-identical rows  */
+                                           /* below the threshold (categories identical;    */
+                                           /* the clustering then sees other rows, so       */
+                                           /* activations agree within FP32 rounding)       */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -201,7 +208,8 @@ int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows);
 int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
 
 /* Rows processed by every layer of the last inference (plain rows for layers
- * below the threshold, centroid + non-empty residue rows above it); out has
+ * below the threshold -- one per set of merged identical rows in SNICIT mode
+ * --, centroid + non-empty residue rows above it); out has
  * room for num_layers entries.  (The reference prints these counts only as
  * debugging output, src/SDGC/XY/XY.hpp:481.) */
 int sdnn_get_layer_rows(const sdnn_engine* e, int64_t* out, int32_t num_layers);
@@ -287,6 +295,12 @@ int sdnn_server_get_stats(sdnn_server* sv, sdnn_server_stats* out);
  * [row_offset, row_offset + rows) of the stream, written to out (rows x N). */
 int sdnn_generate_inputs(int32_t num_neurons, uint64_t seed, int64_t row_offset,
                          int64_t rows, float* out);
+
+/* The same rows generated on the current device into d_out (16-byte
+ * aligned, num_neurons a multiple of 4), asynchronously on `stream` (a
+ * cudaStream_t; NULL = default stream); bitwise equal to the host rows. */
+int sdnn_generate_inputs_device(int32_t num_neurons, uint64_t seed, int64_t row_offset,
+                                int64_t rows, float* d_out, void* stream);
 
 /* One synthetic layer as COO (rows/cols/vals each num_neurons * nnz_per_row). */
 int sdnn_generate_layer_coo(int32_t num_neurons, uint64_t seed, int32_t layer,

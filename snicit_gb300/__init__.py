@@ -4,8 +4,8 @@ The compute path is the CUDA library built in-tree (libsnicit_gb300.so);
 this package only binds it.  See include/snicit_gb300.h for the ABI.
 """
 from ._lib import MODES, SdnnError, load  # noqa: F401
-from .engine import (Engine, coo_to_csr, generate_inputs, generate_layer_coo,  # noqa: F401
-                     generate_layer_csr, read_inputs_tsv, write_categories_tsv,
-                     write_inputs_tsv)
+from .engine import (Engine, coo_to_csr, generate_inputs, generate_inputs_device,  # noqa: F401
+                     generate_layer_coo, generate_layer_csr, read_inputs_tsv,
+                     write_categories_tsv, write_inputs_tsv)
 from .sdgc import BF, SNICIT, SNIG, XY  # noqa: F401
 from .serving import Server, mlp_inputs, request_stream, sparse_mlp  # noqa: F401

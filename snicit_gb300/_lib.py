@@ -13,6 +13,7 @@ MODES = {"BF": 0, "SNIG": 1, "XY": 2, "SNICIT": 3}
 FLAG_NO_BINARY_FIRST_LAYER = 1
 FLAG_NO_PLACEMENT = 2
 FLAG_NO_CHAIN = 4
+FLAG_NO_MERGE = 8
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",
@@ -34,7 +35,8 @@ class Config(ctypes.Structure):
         ("bias", ctypes.c_float), ("clamp", ctypes.c_float), ("num_centroids", ctypes.c_int32),
         ("autotune", ctypes.c_int32), ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
         ("tile_rows", ctypes.c_int32), ("threads", ctypes.c_int32),
-        ("flags", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
+        ("flags", ctypes.c_int32), ("merge_start", ctypes.c_int32),
+        ("merge_every", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
     ]
 
 
@@ -103,6 +105,7 @@ SIGNATURES = [
     ("sdnn_wait", ctypes.c_int, [P, U64, P, P, P, P]),
     ("sdnn_server_get_stats", ctypes.c_int, [P, P]),
     ("sdnn_generate_inputs", ctypes.c_int, [I32, U64, I64, I64, P]),
+    ("sdnn_generate_inputs_device", ctypes.c_int, [I32, U64, I64, I64, P, P]),
     ("sdnn_generate_layer_coo", ctypes.c_int, [I32, U64, I32, I32, F32, P, P, P]),
     ("sdnn_write_weights_tsv", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_write_inputs_tsv", ctypes.c_int, [ctypes.c_char_p, P, I64, I32]),

@@ -35,18 +35,19 @@ __global__ void set_scalar_kernel(int32_t* p, int32_t v) { *p = v; }
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s) { set_scalar_kernel<<<1, 1, 0, s>>>(p, v); }
 
 __global__ void begin_rows_kernel(const int32_t* nrows, int32_t* list, int32_t* count,
-                                  int32_t* zero_a, int32_t* zero_b) {
+                                  int32_t* zero_a, int32_t* zero_b, int32_t* neg) {
   const int n = *nrows;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     list[i] = i;
     if (zero_a) zero_a[i] = 0;
     if (zero_b) zero_b[i] = 0;
+    if (neg) neg[i] = -1;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
 }
 void launch_begin_rows(const int32_t* nrows, int32_t* list, int32_t* count, int32_t* zero_a,
-                       int32_t* zero_b, cudaStream_t s) {
-  begin_rows_kernel<<<264, 256, 0, s>>>(nrows, list, count, zero_a, zero_b);
+                       int32_t* zero_b, int32_t* neg, cudaStream_t s) {
+  begin_rows_kernel<<<264, 256, 0, s>>>(nrows, list, count, zero_a, zero_b, neg);
 }
 
 __global__ void zero_rows_kernel(const int32_t* nrows, int32_t* a, int32_t* b) {
@@ -390,9 +391,11 @@ void launch_recover(const float* y, const int32_t* live, const int32_t* live_cou
 __global__ void materialize_kernel(const float* __restrict__ y, const int32_t* state,
                                    const int32_t* cslot, const int32_t* clist,
                                    const int32_t* is_centroid, const int32_t* res_flag,
-                                   const int32_t* perm, int32_t N, int32_t rows, float* out) {
-  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
-    float* o = out + (size_t)r * N;
+                                   const int32_t* alias, const int32_t* perm, int32_t N,
+                                   int32_t rows, float* out) {
+  for (int ro = blockIdx.x; ro < rows; ro += gridDim.x) {
+    float* o = out + (size_t)ro * N;
+    const int r = alias && alias[ro] >= 0 ? alias[ro] : ro;
     const int st = state[r];
     const float* yr = y + (size_t)r * N;
     if (st == 0) {
@@ -411,9 +414,10 @@ __global__ void materialize_kernel(const float* __restrict__ y, const int32_t* s
 
 void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
                         const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
-                        const int32_t* perm, int32_t N, float* out, int32_t rows, cudaStream_t s) {
+                        const int32_t* alias, const int32_t* perm, int32_t N, float* out,
+                        int32_t rows, cudaStream_t s) {
   materialize_kernel<<<grid_for(rows, 1, 8192), 256, 0, s>>>(y, state, cslot, clist, is_centroid,
-                                                             res_flag, perm, N, rows, out);
+                                                             res_flag, alias, perm, N, rows, out);
 }
 
 // Dense output head on the final activations (dense_output,
@@ -425,16 +429,17 @@ void launch_materialize(const float* y, const int32_t* state, const int32_t* csl
 template <int H>
 __global__ void head_kernel(const float* __restrict__ y, const int32_t* state, const int32_t* cslot,
                             const int32_t* clist, const int32_t* is_centroid,
-                            const int32_t* res_flag, const float* __restrict__ Hp,
-                            const float* __restrict__ hb, int32_t N, int32_t rows, float* logits,
-                            int32_t* argmax) {
+                            const int32_t* res_flag, const int32_t* alias,
+                            const float* __restrict__ Hp, const float* __restrict__ hb, int32_t N,
+                            int32_t rows, float* logits, int32_t* argmax) {
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int r = wid; r < rows; r += nw) {
+  for (int ro = wid; ro < rows; ro += nw) {
     float acc[H];
 #pragma unroll
     for (int k = 0; k < H; ++k) acc[k] = 0.f;
+    const int r = alias && alias[ro] >= 0 ? alias[ro] : ro;
     const int st = state[r];
     if (st != 0) {
       const float* yr = y + (size_t)r * N;
@@ -460,26 +465,26 @@ __global__ void head_kernel(const float* __restrict__ y, const int32_t* state, c
 #pragma unroll
       for (int k = 0; k < H; ++k) {
         const float v = acc[k] + hb[k];
-        logits[(size_t)r * H + k] = v;
+        logits[(size_t)ro * H + k] = v;
         if (k == 0 || v > bv) {
           bv = v;
           best = k;
         }
       }
-      argmax[r] = best;
+      argmax[ro] = best;
     }
   }
 }
 
 bool launch_head(const float* y, const int32_t* state, const int32_t* cslot, const int32_t* clist,
-                 const int32_t* is_centroid, const int32_t* res_flag, const float* Hp,
-                 const float* hb, int32_t H, int32_t N, int32_t rows, float* logits,
-                 int32_t* argmax, cudaStream_t s) {
+                 const int32_t* is_centroid, const int32_t* res_flag, const int32_t* alias,
+                 const float* Hp, const float* hb, int32_t H, int32_t N, int32_t rows,
+                 float* logits, int32_t* argmax, cudaStream_t s) {
   const int grid = grid_for(rows, 8, 2048);
 #define SDNN_HEAD(K)                                                                           \
   case K:                                                                                     \
-    head_kernel<K><<<grid, 256, 0, s>>>(y, state, cslot, clist, is_centroid, res_flag, Hp, hb, N, \
-                                        rows, logits, argmax);                                \
+    head_kernel<K><<<grid, 256, 0, s>>>(y, state, cslot, clist, is_centroid, res_flag, alias, Hp, \
+                                        hb, N, rows, logits, argmax);                         \
     return true;
   switch (H) {
     SDNN_HEAD(1)

@@ -124,6 +124,14 @@ struct sdnn_engine {
   int32_t* d_rows = nullptr;      // row count of the current inference
   int32_t* d_fallback = nullptr;  // layer-0 rows of non-binary tiles
   int32_t* d_fbcount = nullptr;
+  // merging of identical rows (SNICIT, below the threshold)
+  int32_t* d_alias = nullptr;          // [cap] -1 or the row this row was merged into
+  unsigned long long* d_mtable = nullptr;  // [mmask + 1]
+  int32_t* d_mrep = nullptr;           // [mmask + 1]
+  int32_t* d_mpos = nullptr;           // [cap]
+  int32_t* d_mtmp = nullptr;           // [cap]
+  int32_t* d_mcount = nullptr;         // [2]
+  uint32_t mmask = 0;
   int bits_grid = 0;
 
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -209,6 +217,12 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_fallback);
   dfree(e->d_fbcount);
   dfree(e->d_rows);
+  dfree(e->d_alias);
+  dfree(e->d_mtable);
+  dfree(e->d_mrep);
+  dfree(e->d_mpos);
+  dfree(e->d_mtmp);
+  dfree(e->d_mcount);
   if (e->h_counts) cudaFreeHost(e->h_counts);
   e->h_counts = nullptr;
   e->cap = 0;
@@ -228,6 +242,9 @@ constexpr size_t kMaxSmem = 227 * 1024;
 #define SDNN_BITS_THREADS 256
 #endif
 constexpr int kBitsThreads = SDNN_BITS_THREADS;
+// first plain layer after which identical rows are merged (SNICIT): rows are
+// still distinct in the first layers, where most of them die
+constexpr int kMergeStart = 4;
 
 // Chooses chunking, kernel instance, tile rows, threads and grid.
 // Input chunking of the weight layout: whole rows up to 32768 neurons, else
@@ -328,6 +345,20 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_ids, (size_t)cap * 4));
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
+  {
+    uint64_t P = 1024;
+    while (P < 2 * (uint64_t)cap) P <<= 1;
+    e->mmask = (uint32_t)(P - 1);
+    T(A(&e->d_alias, (size_t)cap * 4));
+    T(A(&e->d_mtable, (size_t)P * 8));
+    T(A(&e->d_mrep, (size_t)P * 4));
+    T(A(&e->d_mpos, (size_t)cap * 4));
+    T(A(&e->d_mtmp, (size_t)cap * 4));
+    T(A(&e->d_mcount, 16));
+    if (rc == cudaSuccess) rc = cudaMemset(e->d_mtable, 0, (size_t)P * 8);
+    if (rc == cudaSuccess) rc = cudaMemset(e->d_mrep, 0x7F, (size_t)P * 4);
+    if (rc == cudaSuccess) rc = cudaMemset(e->d_alias, 0xFF, (size_t)cap * 4);
+  }
   T(A(&e->d_fbcount, 16));
   T(A(&e->d_rows, 16));
   if (rc == cudaSuccess) T(cudaMallocHost((void**)&e->h_counts, 16));
@@ -579,6 +610,40 @@ int effective_threshold(const sdnn_engine* e) {
 // and a residue launch per layer), then PH_FINISH (recovery).
 enum Phase { PH_ALL = 0, PH_PRE = 1, PH_POST_LAYERS = 2, PH_POST_CHAIN = 3, PH_FINISH = 4 };
 
+// Merging of identical rows runs in SNICIT mode after plain layer l when
+// merge_start <= l + 1 < T (the threshold clustering covers layer T - 1) and
+// every merge_every layers from there.
+bool merging_on(const sdnn_engine* e) {
+  return e->cfg.mode == SDNN_MODE_SNICIT && !(e->cfg.flags & SDNN_FLAG_NO_MERGE);
+}
+
+bool merge_after(const sdnn_engine* e, int l, int T) {
+  if (!merging_on(e)) return false;
+  const int start = e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart;
+  const int every = e->cfg.merge_every > 0 ? e->cfg.merge_every : 1;
+  const int k = l + 1;
+  return k >= start && k < T && (k - start) % every == 0;
+}
+
+int enqueue_merge(sdnn_engine* e, int l) {
+  DedupArgs m{};
+  m.y = e->d_y[l & 1];
+  m.list = e->d_list[(l + 1) & 1];
+  m.count = e->d_counts + l + 1;
+  m.table = e->d_mtable;
+  m.slot_rep = e->d_mrep;
+  m.pos_slot = e->d_mpos;
+  m.tmp_list = e->d_mtmp;
+  m.tmp_count = e->d_mcount;
+  m.alias = e->d_alias;
+  m.N = e->N;
+  m.mask = e->mmask;
+  launch_dedup(m, e->num_sms, e->stream);
+  e->launches += 3;
+  CK(cudaGetLastError());
+  return SDNN_OK;
+}
+
 int enqueue_plain_layers(sdnn_engine* e, int64_t rows, const float* d_in, int T, bool capturing) {
   const int L = e->L;
   const cudaStream_t s = e->stream;
@@ -617,11 +682,11 @@ int enqueue_plain_layers(sdnn_engine* e, int64_t rows, const float* d_in, int T,
       if ((rc = layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount,
                              e->d_list[1], e->d_counts + 1)))
         return rc;
-      continue;
-    }
-    if ((rc = layer_launch(e, l, EPI_PLAIN, in, e->d_y[l & 1], e->d_list[l & 1], e->d_counts + l,
-                           e->d_list[(l + 1) & 1], e->d_counts + l + 1)))
+    } else if ((rc = layer_launch(e, l, EPI_PLAIN, in, e->d_y[l & 1], e->d_list[l & 1],
+                                  e->d_counts + l, e->d_list[(l + 1) & 1], e->d_counts + l + 1))) {
       return rc;
+    }
+    if (merge_after(e, l, T) && (rc = enqueue_merge(e, l))) return rc;
   }
   if (!(split < T && T == L)) {
     if ((rc = record(e, 1, capturing))) return rc;
@@ -643,7 +708,7 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
   if (phase == PH_ALL || phase == PH_PRE) {
     if ((rc = record(e, 0, capturing))) return rc;
     CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
-    launch_begin_rows(e->d_rows, e->d_list[0], e->d_counts, d_flags, e->d_state, s);
+    launch_begin_rows(e->d_rows, e->d_list[0], e->d_counts, d_flags, e->d_state, e->d_alias, s);
     e->launches++;
     if ((rc = enqueue_plain_layers(e, rows, d_in, T, capturing))) return rc;
   }
@@ -715,6 +780,10 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
                    e->d_resflag, e->N, d_flags, s);
     launch_mark_rows(live, live_count, e->d_state, 2, s);
     e->launches += 3;
+    if (merging_on(e)) {
+      launch_resolve_alias(e->d_rows, e->d_alias, d_flags, L, s);
+      e->launches++;
+    }
     if ((rc = record(e, 4, capturing))) return rc;
   }
   if (phase == PH_ALL) {
@@ -725,6 +794,10 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
     launch_identify(e->d_y[(L - 1) & 1], e->d_list[L & 1], e->d_counts + L, e->N, d_flags, s);
     launch_mark_rows(e->d_list[L & 1], e->d_counts + L, e->d_state, 1, s);
     e->launches += 2;
+    if (merging_on(e)) {  // SNICIT with the threshold at or past the last layer
+      launch_resolve_alias(e->d_rows, e->d_alias, d_flags, L, s);
+      e->launches++;
+    }
     if ((rc = record(e, 4, capturing))) return rc;
   }
   CK(cudaGetLastError());
@@ -1215,7 +1288,8 @@ int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows) {
   const int L = e->L;
   float* scratch = e->d_y[L & 1];
   launch_materialize(e->d_y[(L - 1) & 1], e->d_state, e->d_cslot, e->d_clist, e->d_iscent,
-                     e->d_resflag, e->d_perm_final, e->N, scratch, (int32_t)rows, e->stream);
+                     e->d_resflag, e->d_alias, e->d_perm_final, e->N, scratch, (int32_t)rows,
+                     e->stream);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, scratch, (size_t)rows * e->N * 4, cudaMemcpyDeviceToHost, e->stream));
   CK(cudaStreamSynchronize(e->stream));
@@ -1350,7 +1424,8 @@ std::vector<int32_t> engine_final_positions(const sdnn_engine* e) {
 bool engine_head(sdnn_engine* e, const float* Hp, const float* hb, int32_t H, int64_t rows,
                  float* logits, int32_t* argmax) {
   return launch_head(e->d_y[(e->L - 1) & 1], e->d_state, e->d_cslot, e->d_clist, e->d_iscent,
-                     e->d_resflag, Hp, hb, H, e->N, (int32_t)rows, logits, argmax, e->stream);
+                     e->d_resflag, e->d_alias, Hp, hb, H, e->N, (int32_t)rows, logits, argmax,
+                     e->stream);
 }
 std::string engine_error(const sdnn_engine* e) { return e->err; }
 void engine_set_error(sdnn_engine* e, const std::string& msg) { e->err = msg; }

@@ -122,9 +122,10 @@ cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s);
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s);
-// list[i] = i and zero_a[i] = zero_b[i] = 0 for i < *nrows; *count = *nrows
+// list[i] = i, zero_a[i] = zero_b[i] = 0 and neg[i] = -1 for i < *nrows;
+// *count = *nrows
 void launch_begin_rows(const int32_t* nrows, int32_t* list, int32_t* count, int32_t* zero_a,
-                       int32_t* zero_b, cudaStream_t s);
+                       int32_t* zero_b, int32_t* neg, cudaStream_t s);
 void launch_zero_rows(const int32_t* nrows, int32_t* a, int32_t* b, cudaStream_t s);
 void launch_copy_rows(const int32_t* nrows, const float* src, float* dst, int32_t N, cudaStream_t s);
 void launch_identify(const float* y, const int32_t* list, const int32_t* count, int32_t N,
@@ -164,16 +165,37 @@ void launch_recover(const float* y, const int32_t* live, const int32_t* live_cou
 // Final activations of every row into out[rows][N]: state 0 = dead (zeros),
 // 1 = plain final row, 2 = SNICIT live row (centroid, or centroid + residue).
 // perm[c] = position of neuron c in the final buffer (nullptr = identity).
+// alias[r] >= 0: row r was merged into row alias[r] (read that row instead).
 void launch_materialize(const float* y, const int32_t* state, const int32_t* cslot,
                         const int32_t* clist, const int32_t* is_centroid, const int32_t* res_flag,
-                        const int32_t* perm, int32_t N, float* out, int32_t rows, cudaStream_t s);
+                        const int32_t* alias, const int32_t* perm, int32_t N, float* out,
+                        int32_t rows, cudaStream_t s);
 
 // Dense output head (logits = recovered final row . H + b) for H in
 // {1, 2, 4, 8, 10, 16, 32}; Hp is stored by final position.  False if H is
 // not one of those.
 bool launch_head(const float* y, const int32_t* state, const int32_t* cslot, const int32_t* clist,
-                 const int32_t* is_centroid, const int32_t* res_flag, const float* Hp,
-                 const float* hb, int32_t H, int32_t N, int32_t rows, float* logits,
-                 int32_t* argmax, cudaStream_t s);
+                 const int32_t* is_centroid, const int32_t* res_flag, const int32_t* alias,
+                 const float* Hp, const float* hb, int32_t H, int32_t N, int32_t rows,
+                 float* logits, int32_t* argmax, cudaStream_t s);
+
+// ---- exact merging of identical rows (dedup.cu) ----
+struct DedupArgs {
+  const float* y;               // [rows][N] activations after the layer
+  int32_t* list;                // live rows after the layer; compacted in place
+  int32_t* count;               // its count; rewritten
+  unsigned long long* table;    // [mask + 1] keys, 0 = empty (all empty between calls)
+  int32_t* slot_rep;            // [mask + 1] smallest row per key, 0x7F7F7F7F = empty
+  int32_t* pos_slot;            // [rows] table slot of each list position
+  int32_t* tmp_list;            // [rows]
+  int32_t* tmp_count;           // [2]: kept rows, rows listed before
+  int32_t* alias;               // [rows] -1, or the row this row was merged into
+  int32_t N;
+  uint32_t mask;                // table entries - 1 (a power of 2 >= 2 x rows, minus 1)
+};
+void launch_dedup(const DedupArgs& a, int num_sms, cudaStream_t s);
+// alias[r] := root of r's chain, flags[r] := flags[root] for merged rows.
+void launch_resolve_alias(const int32_t* nrows, int32_t* alias, int32_t* flags, int32_t max_depth,
+                          cudaStream_t s);
 
 }  // namespace sdnn

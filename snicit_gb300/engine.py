@@ -22,7 +22,7 @@ class Engine:
     def __init__(self, num_neurons=1024, num_layers=120, mode="SNICIT", threshold=30,
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
                  device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
-                 chain=True):
+                 chain=True, merge=True, merge_start=0, merge_every=0):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -40,7 +40,10 @@ class Engine:
         cfg.threads = int(threads)
         cfg.flags = ((0 if binary_first_layer else _lib.FLAG_NO_BINARY_FIRST_LAYER)
                      | (0 if placement else _lib.FLAG_NO_PLACEMENT)
-                     | (0 if chain else _lib.FLAG_NO_CHAIN))
+                     | (0 if chain else _lib.FLAG_NO_CHAIN)
+                | (0 if merge else _lib.FLAG_NO_MERGE))
+        cfg.merge_start = int(merge_start)
+        cfg.merge_every = int(merge_every)
         self.cfg = cfg
         self.N = cfg.num_neurons
         self.L = cfg.num_layers
@@ -172,6 +175,13 @@ def generate_inputs(num_neurons, seed, row_offset, rows):
     check(load().sdnn_generate_inputs(int(num_neurons), int(seed), int(row_offset), int(rows),
                                       _ptr(out)))
     return out
+
+
+def generate_inputs_device(num_neurons, seed, row_offset, rows, d_ptr, stream_ptr=None):
+    """Same rows as generate_inputs, written on the current device at d_ptr."""
+    check(load().sdnn_generate_inputs_device(int(num_neurons), int(seed), int(row_offset), int(rows),
+                                             ctypes.c_void_p(int(d_ptr)),
+                                             ctypes.c_void_p(int(stream_ptr)) if stream_ptr else None))
 
 
 def generate_layer_coo(num_neurons, seed, layer, nnz_per_row=32, value=0.0625):

@@ -338,3 +338,61 @@ def test_uneven_batches_in_one_schedule(mode):
     for f, f2, a, b in zip(flags, flags2, alone, batches):
         _, alive, _ = orc.infer(layers, N, -0.3, b, precision=64, want_y=False)
         assert np.array_equal(f, alive) and np.array_equal(f2, alive) and np.array_equal(a, alive)
+
+
+@pytest.mark.parametrize("N,L,B,T", [(1024, 60, 3000, 30), (4096, 40, 1500, 30)])
+def test_row_merging_is_exact(N, L, B, T):
+    """Merging bitwise-identical rows below the threshold keeps the category
+    set, keeps activations within the oracle bound, is deterministic, and
+    computes fewer row-layers than the same SNICIT run without merging."""
+    seed = 23
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    out = {}
+    for merge in (True, False):
+        runs = []
+        for _ in range(2):
+            with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=B, num_centroids=32,
+                           merge=merge, merge_start=2) as eng:
+                eng.generate_weights(seed)
+                flags, ids = eng.infer(Y0)
+                runs.append((flags, ids, eng.activations(B), eng.stats()))
+        assert np.array_equal(runs[0][2], runs[1][2]), f"merge={merge}: not deterministic"
+        out[merge] = runs[0]
+    bias = sg.load().sdnn_reference_bias(N)
+    Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
+    for merge, (flags, ids, Y, st) in out.items():
+        _check(Y, flags, ids, Yref, alive, f"merge={merge}", Y32=Y32)
+    assert out[True][3]["pre_row_layers"] < out[False][3]["pre_row_layers"]
+
+
+def test_duplicate_input_rows_are_merged_and_recovered():
+    """Inputs with repeated rows: the copies end bitwise equal to each other and
+    to the oracle bound, with merging on (they merge at the first merge step)."""
+    N, L, B, T, seed = 1024, 24, 400, 12, 29
+    base = sg.generate_inputs(N, seed, 0, 50)
+    idx = np.random.default_rng(3).integers(0, 50, B)
+    Y0 = base[idx]
+    with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=B, num_centroids=16,
+                   merge_start=1) as eng:
+        eng.generate_weights(seed)
+        flags, ids = eng.infer(Y0)
+        Y = eng.activations(B)
+        rows = eng.layer_rows()
+    for k in range(50):
+        grp = np.flatnonzero(idx == k)
+        if len(grp) > 1:
+            assert np.array_equal(Y[grp], np.repeat(Y[grp[:1]], len(grp), axis=0))
+            assert len(set(flags[grp])) == 1
+    assert rows[1] <= 50, f"rows after the first merge: {rows[1]}"
+    bias = sg.load().sdnn_reference_bias(N)
+    Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
+    _check(Y, flags, ids, Yref, alive, "duplicates", Y32=Y32)
+
+
+@pytest.mark.parametrize("N,off,rows", [(1024, 0, 300), (4096, 12345, 77), (256, 5, 1)])
+def test_device_input_generator_matches_host(N, off, rows):
+    torch = pytest.importorskip("torch")
+    d = torch.empty((rows, N), dtype=torch.float32, device="cuda")
+    sg.generate_inputs_device(N, 99, off, rows, d.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy(), sg.generate_inputs(N, 99, off, rows))
