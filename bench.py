@@ -134,7 +134,13 @@ def cpu_port_rate(sg, N, L, bias, rows_budget_s=12.0, offset=0, layers=None):
 
 def run_reference(args):
     import snicit_gb300 as sg
-    N, L, B, bias, _ = WORKLOADS[args.workload]
+    if args.workload in UNEVEN:
+        import numpy as np
+        N, L, bias, nb, lo, hi = UNEVEN[args.workload]
+        rng = np.random.default_rng([SEED, 6])
+        B = int(np.clip(np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), nb))), lo, hi).sum())
+    else:
+        N, L, B, bias, _ = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -179,31 +185,35 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     N, L, B, bias, t_default = WORKLOADS[args.workload]
     threshold = args.threshold if args.threshold is not None else t_default
-    # each rank runs its own batch (weak scaling over independent samples)
-    Y0 = sg.generate_inputs(N, SEED, rank * B, B)
     edges = float(B) * NNZ * N * L
+    # each rank runs its own batch (weak scaling over independent samples);
+    # the rows are generated on the device (bitwise equal to the host generator)
+    d_in = torch.empty((B, N), dtype=torch.float32, device=dev)
+    sg.generate_inputs_device(N, SEED, rank * B, B, d_in.data_ptr())
+    d_flags = torch.zeros(B, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
 
     eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=B, bias=bias,
                     num_centroids=args.centroids, device=local, tile_rows=args.tile,
                     threads=args.threads)
     eng.generate_weights(SEED, NNZ, 0.0625)
+    t0 = time.perf_counter()
     eng.finalize()
-    tune = None
+    pack_s = time.perf_counter() - t0
     if not args.no_autotune and not args.tile:
         rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
         os.makedirs(os.path.dirname(rec), exist_ok=True)
         if os.path.exists(rec):
             os.remove(rec)
-        tune = eng.autotune(Y0[: args.tune_rows] if args.tune_rows else Y0, rec)
+        rows = args.tune_rows or B
+        eng.autotune_device(d_in.data_ptr(), rows, rec)
 
-    d_in = torch.from_numpy(Y0).to(f"cuda:{local}")
-    d_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
-    torch.cuda.synchronize()
     # a real (non-default) stream: the engine orders its own stream after it and
     # makes it wait for the engine, so events recorded here bracket the work
-    stream = torch.cuda.Stream(device=f"cuda:{local}")
+    stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
 
     def step():
@@ -212,14 +222,13 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    st = eng.stats()
     flags_ref = d_flags.cpu().numpy().copy()
 
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    pre_ms, per_step = [], []
+    per_step = []
     with Clocks(local) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
@@ -245,26 +254,6 @@ def run_ours(args):
     max_ms = float(t.item())
     value = world * edges * args.steps / (max_ms / 1e3)
     ms_per_step = max_ms / args.steps
-
-    # plain per-layer path on the same batch (the comparison point)
-    plain = sg.Engine(N, L, mode="SNIG", batch=B, bias=bias, device=local,
-                      tile_rows=tune["tile_rows"] if tune else args.tile,
-                      threads=tune["threads"] if tune else args.threads)
-    plain.generate_weights(SEED, NNZ, 0.0625)
-    plain_flags = torch.zeros(B, dtype=torch.int32, device=f"cuda:{local}")
-    for _ in range(2):
-        plain.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
-    torch.cuda.synchronize()
-    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    psteps = max(1, min(args.steps, 3))
-    p0.record(stream)
-    for _ in range(psteps):
-        plain.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
-    p1.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = p0.elapsed_time(p1) / psteps
-    pst = plain.stats()
-    plain_exact = bool(np.array_equal(plain_flags.cpu().numpy(), flags))
 
     # roofline of the dominant kernel: the plain layer kernel of the pre-threshold stage
     nnz_layer = st["weight_nnz"] / L
@@ -295,12 +284,13 @@ def run_ours(args):
                 "smem_peak_gbs": smem_gbs}
 
     # end to end through the public host API: pinned host inputs in, survivor ids out
-    pinned = torch.from_numpy(Y0).pin_memory()
-    host = pinned.numpy()
+    host_t = torch.empty((B, N), dtype=torch.float32, pin_memory=True)
+    host_t.copy_(d_in)
+    host = host_t.numpy()
     eng.infer(host, want_flags=False, want_ids=True)
     e2e_t = []
     count = 0
-    for _ in range(max(1, args.steps)):
+    for _ in range(max(1, min(args.steps, 10))):
         t0 = time.perf_counter()
         _, ids = eng.infer(host, want_flags=False, want_ids=True)
         e2e_t.append(time.perf_counter() - t0)
@@ -309,6 +299,24 @@ def run_ours(args):
     e2e_s = statistics.median(e2e_t)
     e2e = {"value": world * edges / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": B * N * 4,
            "d2h_bytes_per_step": 4 + 4 * count, "ms_per_step": e2e_s * 1e3}
+    del host_t, host
+
+    # plain per-layer path (SNIG mode) on the same batch and the same resident weights
+    eng.set_mode("SNIG", L)
+    plain_flags = torch.zeros(B, dtype=torch.int32, device=dev)
+    for _ in range(2):
+        eng.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    psteps = max(1, min(args.steps, 3))
+    p0.record(stream)
+    for _ in range(psteps):
+        eng.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1) / psteps
+    pst = eng.stats()
+    plain_exact = bool(np.array_equal(plain_flags.cpu().numpy(), flags))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -326,7 +334,8 @@ def run_ours(args):
             "config": {"workload": args.workload, "neurons": N, "layers": L, "batch": B,
                        "nnz_per_row": NNZ, "bias": bias, "mode": "SNICIT",
                        "threshold": st["threshold"], "centroids_kept": st["centroids"],
-                       "centroid_candidates": eng.cfg.num_centroids,
+                       "centroid_candidates": st["centroid_candidates"],
+                       "merge_start": st["merge_start"],
                        "tile_rows": st["tile_rows"], "threads": st["threads"],
                        "l2": "inputs (B*N*4 bytes) larger than L2",
                        "parallelism": f"replicas x{world} (independent batches)"},
@@ -334,6 +343,7 @@ def run_ours(args):
             "p99_ms": sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))],
             "survivors": int(flags.sum()),
             "stage_ms": st["stage_ms"],
+            "pack_s": pack_s,
             "plain": {"ms_per_inference": plain_ms, "edges_per_s": edges / (plain_ms / 1e3),
                       "category_set_equal": plain_exact, "row_layers": pst["row_layers"]},
             "speedup_vs_plain": plain_ms / ms_per_step,
@@ -345,9 +355,94 @@ def run_ours(args):
             line["serving"] = run_serving(args, sg, local)
         print(json.dumps(line), flush=True)
     eng.close()
-    plain.close()
     if dist:
         dist.destroy_process_group()
+
+
+UNEVEN = {
+    # name: (N, L, bias, batches, smallest, largest)
+    "uneven-65536x1920": (65536, 1920, -0.45, 12, 500, 60000),
+    "uneven-4096x480": (4096, 480, -0.35, 12, 500, 60000),
+}
+
+
+def run_uneven(args):
+    """Twelve seeded batches of log-uniform sizes run as one launch schedule
+    (sdnn_infer_batches_device) against the same batches one by one."""
+    import numpy as np
+    import torch
+    import snicit_gb300 as sg
+    torch.cuda.set_device(0)
+    N, L, bias, nb, lo, hi = UNEVEN[args.workload]
+    rng = np.random.default_rng([SEED, 6])
+    sizes = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), nb))).astype(np.int64)
+    sizes = np.clip(sizes, lo, hi)
+    total = int(sizes.sum())
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    d_in = torch.empty((total, N), dtype=torch.float32, device="cuda")
+    sg.generate_inputs_device(N, SEED, 0, total, d_in.data_ptr())
+    d_flags = torch.zeros(total, dtype=torch.int32, device="cuda")
+    ptrs = [d_in[offs[i]].data_ptr() for i in range(nb)]
+    fptrs = [d_flags[offs[i]:].data_ptr() for i in range(nb)]
+    eng = sg.Engine(N, L, mode="SNICIT", threshold=30, batch=total, bias=bias,
+                    num_centroids=args.centroids, tile_rows=args.tile, threads=args.threads)
+    eng.generate_weights(SEED, NNZ, 0.0625)
+    t0 = time.perf_counter()
+    eng.finalize()
+    pack_s = time.perf_counter() - t0
+    if not args.no_autotune and not args.tile:
+        rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
+        os.makedirs(os.path.dirname(rec), exist_ok=True)
+        if os.path.exists(rec):
+            os.remove(rec)
+        eng.autotune_device(ptrs[int(np.argmax(sizes))], int(sizes.max()), rec)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def together():
+        eng.infer_batches_device(ptrs, sizes, fptrs, stream.cuda_stream)
+
+    def one_by_one():
+        for p, n, f in zip(ptrs, sizes, fptrs):
+            eng.infer_device(p, int(n), f, stream.cuda_stream)
+
+    res = {}
+    for name, fn in (("one_schedule", together), ("one_by_one", one_by_one)):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(0) as clk:
+            ev0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        res[name] = {"ms": ms, "flags": d_flags.cpu().numpy().copy(), "clocks": clk.summary(),
+                     "stats": eng.stats()}
+    same = bool(np.array_equal(res["one_schedule"]["flags"], res["one_by_one"]["flags"]))
+    edges = float(total) * NNZ * N * L
+    st = res["one_schedule"]["stats"]
+    line = {
+        "metric": METRIC, "value": edges / (res["one_schedule"]["ms"] / 1e3), "unit": "edges/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": res["one_schedule"]["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "neurons": N, "layers": L, "batch_sizes": sizes.tolist(),
+                   "rows": total, "bias": bias, "mode": "SNICIT", "threshold": st["threshold"],
+                   "tile_rows": st["tile_rows"], "threads": st["threads"],
+                   "merge_start": st["merge_start"]},
+        "one_by_one": {"ms_per_step": res["one_by_one"]["ms"],
+                       "edges_per_s": edges / (res["one_by_one"]["ms"] / 1e3)},
+        "speedup_vs_one_by_one": res["one_by_one"]["ms"] / res["one_schedule"]["ms"],
+        "category_sets_equal": same, "survivors": int(res["one_schedule"]["flags"].sum()),
+        "stage_ms": st["stage_ms"], "pack_s": pack_s,
+        "gpu_launches": st["launches"] * args.steps,
+        "clocks": res["one_schedule"]["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
 
 
 def _percentile(xs, q):
@@ -451,7 +546,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sdgc-4096x480", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="sdgc-4096x480", choices=sorted(WORKLOADS) + sorted(UNEVEN))
     ap.add_argument("--threshold", type=int, default=None)
     ap.add_argument("--centroids", type=int, default=50)
     ap.add_argument("--tune-rows", type=int, default=0, help="rows used by the autotuner (0 = all)")
@@ -474,6 +569,8 @@ def main():
         print(json.dumps({"serving": run_serving(args, sg)}), flush=True)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.workload in UNEVEN:
+        run_uneven(args)
     else:
         run_ours(args)
 

@@ -110,7 +110,9 @@ typedef struct sdnn_stats {
   int64_t pre_row_layers;   /* rows processed by the plain layers (sum)        */
   int64_t post_row_layers;  /* centroid + residue rows of the post layers      */
   int64_t weight_nnz;       /* nonzeros of all L layers                        */
-  int32_t reserved[4];
+  int32_t centroid_candidates; /* candidates drawn at the threshold (setting)        */
+  int32_t merge_start;   /* first layer after which identical rows are merged     */
+  int32_t reserved[2];
 } sdnn_stats;
 
 typedef struct sdnn_engine sdnn_engine;
@@ -207,6 +209,11 @@ int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows);
 /* Statistics of the last inference. */
 int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
 
+/* Switches the mode (and threshold) of an engine without repacking its
+ * weights, e.g. to time the plain path and SNICIT on one resident copy of W.
+ * (The reference picks the engine class once, main/SDGC.cu:104-110.) */
+int sdnn_set_mode(sdnn_engine* e, int32_t mode, int32_t threshold);
+
 /* Rows processed by every layer of the last inference (plain rows for layers
  * below the threshold -- one per set of merged identical rows in SNICIT mode
  * --, centroid + non-empty residue rows above it); out has
@@ -235,6 +242,10 @@ int sdnn_layer_noalloc(sdnn_engine* e, int32_t layer, const float* d_y_in, float
  * on the given sample rows (host buffer) and appends one JSON line per tried
  * setting to record_path (if not NULL).  Applies the fastest setting. */
 int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows, const char* record_path);
+/* The same on device-resident sample rows (d_Y0: rows x N, 16-byte aligned);
+ * SNICIT mode also sweeps the first merge layer of identical rows. */
+int sdnn_autotune_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
+                         const char* record_path);
 
 /* ---- serving: continuous batching of requests ---------------------------- */
 

@@ -49,7 +49,8 @@ class Stats(ctypes.Structure):
         ("threshold", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
         ("threads", ctypes.c_int32), ("reserved0", ctypes.c_int32),
         ("pre_row_layers", ctypes.c_int64), ("post_row_layers", ctypes.c_int64),
-        ("weight_nnz", ctypes.c_int64), ("reserved", ctypes.c_int32 * 4),
+        ("weight_nnz", ctypes.c_int64), ("centroid_candidates", ctypes.c_int32),
+        ("merge_start", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
     ]
 
 
@@ -95,6 +96,8 @@ SIGNATURES = [
     ("sdnn_get_stats", ctypes.c_int, [P, P]),
     ("sdnn_get_layer_rows", ctypes.c_int, [P, P, I32]),
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
+    ("sdnn_autotune_device", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
+    ("sdnn_set_mode", ctypes.c_int, [P, I32, I32]),
     ("sdnn_layer_noalloc", ctypes.c_int, [P, I32, P, P, I64, P, P]),
     ("sdnn_server_config_default", ctypes.c_int, [P]),
     ("sdnn_server_create", ctypes.c_int, [P, P, P, P, P]),

@@ -11,32 +11,55 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "snicit_gb300.h"
 
 namespace sdnn {
 int engine_set_tile(sdnn_engine* e, int tile_rows, int threads);
 void engine_set_snicit(sdnn_engine* e, int threshold, int centroids);
+void engine_set_merge(sdnn_engine* e, int start, int every, bool on);
 sdnn_config engine_config(const sdnn_engine* e);
 }  // namespace sdnn
 
 namespace {
 
 struct Trial {
-  int tile, threads, threshold, centroids;
+  int tile, threads, threshold, centroids, merge_start;
   float ms;
   int64_t survivors;
   int status;
 };
 
+// One inference of the sample: host rows (copied in) or device rows.
+struct Sample {
+  const float* host = nullptr;
+  const float* dev = nullptr;
+  int64_t rows = 0;
+  int32_t* d_flags = nullptr;  // device path: flags buffer
+};
+
+int run_once(sdnn_engine* e, const Sample& smp, int64_t& survivors) {
+  if (smp.host) return sdnn_infer_host(e, smp.host, smp.rows, nullptr, nullptr, &survivors);
+  int rc = sdnn_infer_device(e, smp.dev, smp.rows, smp.d_flags, nullptr);
+  if (rc) return rc;
+  std::vector<int32_t> flags((size_t)smp.rows);
+  if (cudaDeviceSynchronize() != cudaSuccess ||
+      cudaMemcpy(flags.data(), smp.d_flags, flags.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return SDNN_ERR_CUDA;
+  survivors = 0;
+  for (int32_t v : flags) survivors += v != 0;
+  return SDNN_OK;
+}
+
 // Times one setting: best of two runs after a warm-up (which captures the
 // graph).  stage < 0 times the whole inference, else that stage only (the
 // tile sweep times the plain layers, stage 0, where the tile shape matters).
-int time_setting(sdnn_engine* e, const float* Y0, int64_t rows, int stage, float& ms,
-                 int64_t& survivors) {
+int time_setting(sdnn_engine* e, const Sample& smp, int stage, float& ms, int64_t& survivors) {
   float best = 1e30f;
   for (int rep = 0; rep < 3; ++rep) {
     int64_t count = 0;
-    int rc = sdnn_infer_host(e, Y0, rows, nullptr, nullptr, &count);
+    int rc = run_once(e, smp, count);
     if (rc) return rc;
     sdnn_stats st{};
     rc = sdnn_get_stats(e, &st);
@@ -53,18 +76,14 @@ void record(FILE* f, const char* phase, const Trial& t, int64_t rows) {
   if (!f) return;
   std::fprintf(f,
                "{\"phase\": \"%s\", \"tile_rows\": %d, \"threads\": %d, \"threshold\": %d, "
-               "\"centroids\": %d, \"rows\": %lld, \"ms\": %.4f, \"survivors\": %lld, "
-               "\"status\": %d}\n",
-               phase, t.tile, t.threads, t.threshold, t.centroids, (long long)rows, t.ms,
-               (long long)t.survivors, t.status);
+               "\"centroids\": %d, \"merge_start\": %d, \"rows\": %lld, \"ms\": %.4f, "
+               "\"survivors\": %lld, \"status\": %d}\n",
+               phase, t.tile, t.threads, t.threshold, t.centroids, t.merge_start, (long long)rows,
+               t.ms, (long long)t.survivors, t.status);
   std::fflush(f);
 }
 
-}  // namespace
-
-extern "C" int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows,
-                             const char* record_path) {
-  if (!e || !Y0 || rows <= 0) return SDNN_ERR_INVALID;
+int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
   FILE* f = record_path ? std::fopen(record_path, "ab") : nullptr;
   const sdnn_config cfg0 = sdnn::engine_config(e);
   const int N = cfg0.num_neurons;
@@ -74,20 +93,19 @@ extern "C" int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows,
   else if (N == 16384) tiles = {3, 2, 1};
   else if (N > 32768) tiles = {3, 2, 1};
   else tiles = {8, 4, 2, 1};
-  Trial best{0, 0, cfg0.threshold, cfg0.num_centroids, 1e30f, -1, 0};
+  const bool merge_on = !(cfg0.flags & SDNN_FLAG_NO_MERGE);
+  Trial best{0, 0, cfg0.threshold, cfg0.num_centroids, cfg0.merge_start, 1e30f, -1, 0};
   // the plain layers (stage 0) are where the tile shape matters; in SNICIT mode
   // the post layers run a handful of rows whatever the tile
   const int tile_stage =
       (cfg0.mode == SDNN_MODE_SNICIT && cfg0.threshold > 0 && cfg0.threshold < cfg0.num_layers) ? 0 : -1;
-  int64_t ref_survivors = -1;
   for (int tile : tiles) {
     for (int threads : {256, 512}) {
-      Trial t{tile, threads, cfg0.threshold, cfg0.num_centroids, 0.f, 0, 0};
+      Trial t{tile, threads, cfg0.threshold, cfg0.num_centroids, cfg0.merge_start, 0.f, 0, 0};
       t.status = sdnn::engine_set_tile(e, tile, threads);
-      if (t.status == SDNN_OK) t.status = time_setting(e, Y0, rows, tile_stage, t.ms, t.survivors);
-      record(f, "tile", t, rows);
+      if (t.status == SDNN_OK) t.status = time_setting(e, smp, tile_stage, t.ms, t.survivors);
+      record(f, "tile", t, smp.rows);
       if (t.status != SDNN_OK) continue;
-      if (ref_survivors < 0) ref_survivors = t.survivors;
       if (t.ms < best.ms) best = t;
     }
   }
@@ -104,16 +122,55 @@ extern "C" int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows,
       if (th >= cfg0.num_layers) continue;
       for (int k : {50, 100, 200}) {
         sdnn::engine_set_snicit(e, th, k);
-        Trial t{best.tile, best.threads, th, k, 0.f, 0, 0};
-        t.status = time_setting(e, Y0, rows, -1, t.ms, t.survivors);
-        record(f, "snicit", t, rows);
+        Trial t{best.tile, best.threads, th, k, cfg0.merge_start, 0.f, 0, 0};
+        t.status = time_setting(e, smp, -1, t.ms, t.survivors);
+        record(f, "snicit", t, smp.rows);
         if (t.status != SDNN_OK) continue;
         if (t.ms < bs.ms) bs = t;
       }
     }
     if (bs.ms < 1e30f) sdnn::engine_set_snicit(e, bs.threshold, bs.centroids);
     else sdnn::engine_set_snicit(e, cfg0.threshold, cfg0.num_centroids);
+    if (merge_on && bs.ms < 1e30f) {
+      // first layer after which identical rows are merged: early merging finds
+      // duplicates sooner, late merging skips hashing rows that are all distinct
+      Trial bm = bs;
+      for (int ms : {2, 3, 6, 8}) {
+        sdnn::engine_set_merge(e, ms, cfg0.merge_every, true);
+        Trial t{bs.tile, bs.threads, bs.threshold, bs.centroids, ms, 0.f, 0, 0};
+        t.status = time_setting(e, smp, -1, t.ms, t.survivors);
+        record(f, "merge", t, smp.rows);
+        if (t.status == SDNN_OK && t.ms < bm.ms) bm = t;
+      }
+      sdnn::engine_set_merge(e, bm.merge_start, cfg0.merge_every, true);
+    }
   }
   if (f) std::fclose(f);
   return SDNN_OK;
+}
+
+}  // namespace
+
+extern "C" int sdnn_autotune(sdnn_engine* e, const float* Y0, int64_t rows,
+                             const char* record_path) {
+  if (!e || !Y0 || rows <= 0) return SDNN_ERR_INVALID;
+  Sample smp;
+  smp.host = Y0;
+  smp.rows = rows;
+  return tune(e, smp, record_path);
+}
+
+extern "C" int sdnn_autotune_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
+                                    const char* record_path) {
+  if (!e || !d_Y0 || rows <= 0) return SDNN_ERR_INVALID;
+  Sample smp;
+  smp.dev = d_Y0;
+  smp.rows = rows;
+  if (cudaMalloc((void**)&smp.d_flags, (size_t)rows * 4) != cudaSuccess) {
+    cudaGetLastError();
+    return SDNN_ERR_OOM;
+  }
+  const int rc = tune(e, smp, record_path);
+  cudaFree(smp.d_flags);
+  return rc;
 }

@@ -964,6 +964,8 @@ int collect_stats(sdnn_engine* e) {
   st.threshold = T;
   st.tile_rows = e->key.T;
   st.threads = e->threads;
+  st.centroid_candidates = e->cfg.num_centroids;
+  st.merge_start = merging_on(e) ? (e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart) : 0;
   e->pending_stats = 0;
   return SDNN_OK;
 }
@@ -1309,6 +1311,14 @@ int sdnn_get_stats(const sdnn_engine* ce, sdnn_stats* out) {
   return SDNN_OK;
 }
 
+int sdnn_set_mode(sdnn_engine* e, int32_t mode, int32_t threshold) {
+  if (!e || mode < SDNN_MODE_BF || mode > SDNN_MODE_SNICIT || threshold < 0) return SDNN_ERR_INVALID;
+  e->cfg.mode = mode;
+  e->cfg.threshold = threshold;
+  drop_graph(e);
+  return SDNN_OK;
+}
+
 int sdnn_get_layer_rows(const sdnn_engine* ce, int64_t* out, int32_t num_layers) {
   if (!ce || !out || num_layers < ce->L) return SDNN_ERR_INVALID;
   auto* e = const_cast<sdnn_engine*>(ce);
@@ -1361,6 +1371,12 @@ void engine_set_snicit(sdnn_engine* e, int threshold, int centroids) {
     e->cfg.num_centroids = centroids;
     free_buffers(e);
   }
+  drop_graph(e);
+}
+void engine_set_merge(sdnn_engine* e, int start, int every, bool on) {
+  e->cfg.merge_start = start;
+  e->cfg.merge_every = every;
+  e->cfg.flags = on ? (e->cfg.flags & ~SDNN_FLAG_NO_MERGE) : (e->cfg.flags | SDNN_FLAG_NO_MERGE);
   drop_graph(e);
 }
 sdnn_config engine_config(const sdnn_engine* e) { return e->cfg; }

@@ -153,13 +153,27 @@ class Engine:
             "residue_rows": s.residue_rows, "launches": s.launches, "threshold": s.threshold,
             "tile_rows": s.tile_rows, "threads": s.threads,
             "pre_row_layers": s.pre_row_layers, "post_row_layers": s.post_row_layers,
-            "weight_nnz": s.weight_nnz,
+            "weight_nnz": s.weight_nnz, "centroid_candidates": s.centroid_candidates,
+            "merge_start": s.merge_start,
         }
 
     def layer_rows(self):
         out = np.zeros(self.L, dtype=np.int64)
         self._ck(load().sdnn_get_layer_rows(self._h, _ptr(out), self.L))
         return out
+
+    def set_mode(self, mode, threshold=None):
+        """Switches mode (and threshold) keeping the packed weights."""
+        m = _lib.MODES[mode] if isinstance(mode, str) else int(mode)
+        t = self.cfg.threshold if threshold is None else int(threshold)
+        self._ck(load().sdnn_set_mode(self._h, m, t))
+        self.cfg.mode = m
+        self.cfg.threshold = t
+
+    def autotune_device(self, d_ptr, rows, record_path=None):
+        """Autotuner on device-resident sample rows (applies the fastest setting)."""
+        self._ck(load().sdnn_autotune_device(self._h, ctypes.c_void_p(int(d_ptr)), int(rows),
+                                             str(record_path).encode() if record_path else None))
 
     def autotune(self, Y0, record_path=None):
         Y0 = np.ascontiguousarray(Y0, dtype=np.float32)

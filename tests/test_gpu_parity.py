@@ -396,3 +396,25 @@ def test_device_input_generator_matches_host(N, off, rows):
     sg.generate_inputs_device(N, 99, off, rows, d.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(d.cpu().numpy(), sg.generate_inputs(N, 99, off, rows))
+
+
+def test_set_mode_and_device_autotune():
+    """One resident copy of W serves SNICIT and the plain path; the device-side
+    autotuner keeps the category set."""
+    torch = pytest.importorskip("torch")
+    N, L, B, seed = 1024, 64, 2000, 41
+    d = torch.empty((B, N), dtype=torch.float32, device="cuda")
+    sg.generate_inputs_device(N, seed, 0, B, d.data_ptr())
+    f = torch.zeros(B, dtype=torch.int32, device="cuda")
+    _, alive, _ = orc.infer(_layers(N, L, seed), N, -0.3, sg.generate_inputs(N, seed, 0, B),
+                            precision=64, want_y=False)
+    with sg.Engine(N, L, mode="SNICIT", threshold=30, batch=B, bias=-0.3) as eng:
+        eng.generate_weights(seed)
+        eng.autotune_device(d.data_ptr(), B)
+        assert eng.stats()["threshold"] in (30, 60)
+        for mode, t in (("SNICIT", 30), ("SNIG", L), ("BF", L), ("SNICIT", 60)):
+            eng.set_mode(mode, t)
+            f.zero_()
+            eng.infer_device(d.data_ptr(), B, f.data_ptr())
+            torch.cuda.synchronize()
+            assert np.array_equal(f.cpu().numpy(), alive), mode
