@@ -335,7 +335,8 @@ def run_ours(args):
                        "nnz_per_row": NNZ, "bias": bias, "mode": "SNICIT",
                        "threshold": st["threshold"], "centroids_kept": st["centroids"],
                        "centroid_candidates": st["centroid_candidates"],
-                       "merge_start": st["merge_start"],
+                       "merge_start": st["merge_start"], "merge_every": st["merge_every"],
+                       "post_kernel": st["post_kernel"],
                        "tile_rows": st["tile_rows"], "threads": st["threads"],
                        "l2": "inputs (B*N*4 bytes) larger than L2",
                        "parallelism": f"replicas x{world} (independent batches)"},

@@ -91,6 +91,8 @@ typedef struct sdnn_config {
                                            /* below the threshold (categories identical;    */
                                            /* the clustering then sees other rows, so       */
                                            /* activations agree within FP32 rounding)       */
+#define SDNN_FLAG_NO_CHAIN_STREAM 16       /* chain kernel reads weights from L2 instead  */
+                                           /* of streaming them into shared memory        */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -112,7 +114,10 @@ typedef struct sdnn_stats {
   int64_t weight_nnz;       /* nonzeros of all L layers                        */
   int32_t centroid_candidates; /* candidates drawn at the threshold (setting)        */
   int32_t merge_start;   /* first layer after which identical rows are merged     */
-  int32_t reserved[2];
+  int32_t merge_every;   /* ... and the spacing of the following merge steps      */
+  int32_t post_kernel;   /* post-threshold path: 0 none, 1 a centroid and a residue
+                            launch per layer, 2 chain kernel (weights from L2),
+                            3 chain kernel (weights streamed to shared memory)    */
 } sdnn_stats;
 
 typedef struct sdnn_engine sdnn_engine;

@@ -14,6 +14,7 @@ FLAG_NO_BINARY_FIRST_LAYER = 1
 FLAG_NO_PLACEMENT = 2
 FLAG_NO_CHAIN = 4
 FLAG_NO_MERGE = 8
+FLAG_NO_CHAIN_STREAM = 16
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",
@@ -50,7 +51,8 @@ class Stats(ctypes.Structure):
         ("threads", ctypes.c_int32), ("reserved0", ctypes.c_int32),
         ("pre_row_layers", ctypes.c_int64), ("post_row_layers", ctypes.c_int64),
         ("weight_nnz", ctypes.c_int64), ("centroid_candidates", ctypes.c_int32),
-        ("merge_start", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
+        ("merge_start", ctypes.c_int32), ("merge_every", ctypes.c_int32),
+        ("post_kernel", ctypes.c_int32),
     ]
 
 

@@ -134,15 +134,22 @@ int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
     if (merge_on && bs.ms < 1e30f) {
       // first layer after which identical rows are merged: early merging finds
       // duplicates sooner, late merging skips hashing rows that are all distinct
+      // (merging after every layer, or every second one: half the hashing)
       Trial bm = bs;
-      for (int ms : {2, 3, 6, 8}) {
-        sdnn::engine_set_merge(e, ms, cfg0.merge_every, true);
-        Trial t{bs.tile, bs.threads, bs.threshold, bs.centroids, ms, 0.f, 0, 0};
-        t.status = time_setting(e, smp, -1, t.ms, t.survivors);
-        record(f, "merge", t, smp.rows);
-        if (t.status == SDNN_OK && t.ms < bm.ms) bm = t;
+      int best_every = cfg0.merge_every;
+      for (int every : {1, 2}) {
+        for (int ms : {2, 4, 6, 8, 10}) {
+          sdnn::engine_set_merge(e, ms, every, true);
+          Trial t{bs.tile, bs.threads, bs.threshold, bs.centroids, ms, 0.f, 0, 0};
+          t.status = time_setting(e, smp, -1, t.ms, t.survivors);
+          record(f, every == 1 ? "merge" : "merge_every2", t, smp.rows);
+          if (t.status == SDNN_OK && t.ms < bm.ms) {
+            bm = t;
+            best_every = every;
+          }
+        }
       }
-      sdnn::engine_set_merge(e, bm.merge_start, cfg0.merge_every, true);
+      sdnn::engine_set_merge(e, bm.merge_start, best_every, true);
     }
   }
   if (f) std::fclose(f);

@@ -43,6 +43,7 @@ struct DevLayer {
   int64_t nnz = 0;
   int64_t slots = 0;
   int32_t max_depth = 0;
+  uint32_t chain_slice = 0;  // largest per-CTA weight slice for the chain kernels
 };
 
 struct GraphKey {
@@ -142,7 +143,9 @@ struct sdnn_engine {
   int32_t* h_counts = nullptr;  // pinned: residue rows and centroids after clustering
   int chain_cap = 0;            // centroid rows the cluster chain kernel can carry
   int chain_kc = 1;
+  uint32_t chain_wcap = 0;      // streamed weight buffer of the chain kernel (bytes)
   bool last_chain = false;
+  int last_post_kernel = 0;     // stats: 0 none, 1 per-layer launches, 2/3 chain kernel 1/2
   LayerDev* d_layer_table = nullptr;  // device copy of every layer's descriptor
 
   // last run
@@ -413,6 +416,7 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   d.nnz = p.nnz;
   d.slots = p.slots;
   d.max_depth = p.max_depth;
+  if (e->nq == 1) d.chain_slice = chain_slice_bytes(p.grp_blk.data(), e->G, !p.constw);
   cudaError_t rc = cudaSuccess;
   auto T = [&](cudaError_t r) {
     if (rc == cudaSuccess) rc = r;
@@ -540,6 +544,8 @@ int finalize_weights(sdnn_engine* e) {
     CK(cudaMemcpy(e->d_layer_table, table.data(), sizeof(LayerDev) * e->L, cudaMemcpyHostToDevice));
   }
   e->chain_cap = e->nq == 1 ? chain_capacity(e->N) : 0;
+  e->chain_wcap = 0;
+  for (const DevLayer& d : e->dl) e->chain_wcap = std::max(e->chain_wcap, d.chain_slice);
   if (!e->pos.empty()) {
     CK(cudaMalloc((void**)&e->d_perm_final, (size_t)e->N * 4));
     CK(cudaMemcpy(e->d_perm_final, e->pos[e->L - 1].data(), (size_t)e->N * 4,
@@ -769,6 +775,8 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
     ca.N = e->N;
     ca.G = e->G;
     ca.clampv = e->cfg.clamp;
+    ca.err = e->d_err;
+    ca.wcap = (e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM) ? 0u : e->chain_wcap;
     CK(launch_chain(ca, e->chain_kc, s));
     e->launches++;
     if ((rc = record(e, 3, capturing))) return rc;
@@ -859,6 +867,7 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   e->run_launches++;
   int rc;
   if (e->cfg.mode != SDNN_MODE_SNICIT || T >= e->L) {
+    e->last_post_kernel = 0;
     if ((rc = run_phase(e, 0, PH_ALL, rows, d_in, d_flags))) return rc;
   } else {
     if ((rc = run_phase(e, 1, PH_PRE, rows, d_in, d_flags))) return rc;
@@ -877,6 +886,14 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
       if ((rc = run_phase(e, 3, PH_POST_LAYERS, rows, d_in, d_flags))) return rc;
     }
     e->last_chain = chain;
+    e->last_post_kernel = 1;
+    if (chain) {
+      ChainArgs ca{};
+      ca.N = e->N;
+      ca.G = e->G;
+      ca.wcap = (e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM) ? 0u : e->chain_wcap;
+      e->last_post_kernel = 1 + chain_variant(ca, e->chain_kc);
+    }
     if ((rc = run_phase(e, 4, PH_FINISH, rows, d_in, d_flags))) return rc;
   }
   e->launches = e->run_launches;
@@ -966,6 +983,8 @@ int collect_stats(sdnn_engine* e) {
   st.threads = e->threads;
   st.centroid_candidates = e->cfg.num_centroids;
   st.merge_start = merging_on(e) ? (e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart) : 0;
+  st.merge_every = merging_on(e) ? std::max(1, e->cfg.merge_every) : 0;
+  st.post_kernel = e->last_post_kernel;
   e->pending_stats = 0;
   return SDNN_OK;
 }
@@ -1176,19 +1195,19 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows, int32_t* flag
     if (rc) return rc;
     rc = collect_stats(e);
     if (rc) return rc;
+    if (off == 0) {
+      acc = e->stats;  // settings of the run (threshold, tile, merge, post path, ...)
+      continue;
+    }
     for (int i = 0; i < 4; ++i) acc.stage_ms[i] += e->stats.stage_ms[i];
     acc.total_ms += e->stats.total_ms;
     acc.rows_in += e->stats.rows_in;
     acc.row_layers += e->stats.row_layers;
     acc.pre_row_layers += e->stats.pre_row_layers;
     acc.post_row_layers += e->stats.post_row_layers;
-    acc.weight_nnz = e->stats.weight_nnz;
     acc.centroids = e->stats.centroids;
     acc.residue_rows += e->stats.residue_rows;
     acc.launches += e->stats.launches;
-    acc.threshold = e->stats.threshold;
-    acc.tile_rows = e->stats.tile_rows;
-    acc.threads = e->stats.threads;
   }
   acc.rows_out = total;
   e->stats = acc;

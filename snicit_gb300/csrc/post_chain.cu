@@ -17,6 +17,8 @@
 //    the cluster (distributed shared memory);
 //  * a cluster barrier separates layers; after the last layer the rows go to
 //    the final activation buffer for recovery.
+#include <algorithm>
+
 #include <cooperative_groups.h>
 
 #include "layer_kernel.cuh"
@@ -90,6 +92,224 @@ __global__ void __launch_bounds__(512, 1) chain_kernel(const ChainArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// chain2_kernel: the same computation with the weights of the next layer
+// streamed into shared memory and point-to-point row exchange.
+//
+//  * one producer warp (the last warp of the CTA) runs a layer ahead of the
+//    16 compute warps: as soon as the inputs of layer l are complete (so no
+//    warp still reads the weights of layer l - 1) it copies this CTA's slot
+//    blocks of layer l + 1 into the free one of two weight buffers with a 1-D
+//    TMA bulk copy (and the group offsets with plain loads), so the compute
+//    warps read indices from shared memory instead of waiting on L2;
+//  * outputs go to every CTA of the cluster with st.async, each signalling
+//    the receiving CTA's mbarrier for its next row buffer with 4 bytes; a CTA
+//    starts layer l + 1 when all N x K values of its next buffer have
+//    arrived -- no cluster-wide barrier per layer;
+//  * three row buffers: a CTA that has started layer l + 1 knows every CTA
+//    finished layer l - 1 (it received all of their layer-l outputs), so the
+//    buffer it writes for layer l + 2 is no longer read anywhere.
+// Same slots, same FMA order as layer_kernel and chain_kernel: bitwise equal.
+constexpr int kChain2ComputeWarps = 16;
+constexpr int kChain2MaxGroups = 64;  // groups per CTA (G / cluster size)
+
+__device__ __forceinline__ uint32_t mapa_u32(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_async_f32(uint32_t raddr, float v, uint32_t rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(
+                   raddr),
+               "r"(__float_as_uint(v)), "r"(rbar)
+               : "memory");
+}
+// Bounded wait shared by all threads; after a timeout (error word set) every
+// later wait of this thread is skipped so the kernel runs to its end.
+__device__ __forceinline__ void chain_wait(uint64_t* bar, uint32_t parity, bool& failed,
+                                           int32_t* err) {
+  if (failed) return;
+  if (!mbar_wait_bounded(bar, parity, err)) failed = true;
+}
+
+template <int KC, int RSW, bool CONSTW>
+__device__ __forceinline__ void accumulate_smem(float (&acc)[KC], const uint2* __restrict__ sidx,
+                                                const float4* __restrict__ sval, int nb, float wc,
+                                                const float* __restrict__ ys, int lane) {
+  int b = 0;
+  for (; b + 8 <= nb; b += 8) {
+    uint2 iv[8];
+    float4 vv[CONSTW ? 1 : 8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      iv[k] = sidx[(b + k) * 32 + lane];
+      if constexpr (!CONSTW) vv[k] = sval[(b + k) * 32 + lane];
+    }
+    apply_blocks<KC, RSW, CONSTW, 8>(acc, iv, vv, wc, ys, RSW);
+  }
+  for (; b < nb; ++b) {
+    uint2 iv[1];
+    float4 vv[1];
+    iv[0] = sidx[b * 32 + lane];
+    if constexpr (!CONSTW) vv[0] = sval[b * 32 + lane];
+    apply_blocks<KC, RSW, CONSTW, 1>(acc, iv, vv, wc, ys, RSW);
+  }
+}
+
+template <int RSW, int KC>
+__global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kernel(const ChainArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* rows = reinterpret_cast<float*>(smem);  // [3][KC][RSW]
+  unsigned char* wbase = smem + (size_t)3 * KC * RSW * 4;  // [2][wcap]
+  __shared__ __align__(8) uint64_t rb[3];
+  __shared__ __align__(8) uint64_t wb[2];
+  __shared__ int32_t s_gb[2][kChain2MaxGroups + 1];
+  __shared__ LayerDev s_wl[2];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int csize = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool producer = warp == kChain2ComputeWarps;
+  const int N = a.N;
+  const int K = min(*a.ccount, KC);
+  const int gbeg = (int)((long)a.G * rank / csize), gend = (int)((long)a.G * (rank + 1) / csize);
+  const int ng = gend - gbeg;
+  const uint32_t row_bytes = (uint32_t)K * (uint32_t)N * 4u;
+  bool failed = false;
+
+  auto load_bounds = [&](int l, int32_t* dst) {  // producer warp
+    const int32_t* gb = a.layers[l].grp_blk + gbeg;
+    for (int i = lane; i <= ng; i += 32) dst[i] = __ldg(gb + i);
+  };
+  int wcnt[2] = {0, 0};  // producer: copies issued into each weight buffer
+  auto issue_weights = [&](int l, int buf) {  // producer lane 0, after load_bounds + syncwarp
+    const LayerDev wl = a.layers[l];
+    s_wl[buf] = wl;  // published to the compute warps by the arrive below
+    ++wcnt[buf];
+    const int32_t b0 = s_gb[buf][0], nblk = s_gb[buf][ng] - b0;
+    const uint32_t bi = (uint32_t)nblk * 32u * 8u;
+    const uint32_t bv = wl.val ? (uint32_t)nblk * 32u * 16u : 0u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&wb[buf], bi + bv);
+    unsigned char* dst = wbase + (size_t)buf * a.wcap;
+    if (bi) bulk_g2s(dst, wl.idx + (size_t)b0 * 32, bi, &wb[buf]);
+    if (bv) bulk_g2s(dst + bi, wl.val + (size_t)b0 * 32, bv, &wb[buf]);
+  };
+  auto prefetch_l2 = [&](int l) {  // producer lane 0
+    if (l >= a.last) return;
+    const LayerDev wp = a.layers[l];
+    const int32_t b0 = __ldg(wp.grp_blk + gbeg), b1 = __ldg(wp.grp_blk + gend);
+    const uint32_t bytes = (uint32_t)(b1 - b0) * 32u * (uint32_t)sizeof(uint2);
+    if (bytes > 0)
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wp.idx + (size_t)b0 * 32),
+                   "r"(bytes)
+                   : "memory");
+    if (wp.val && bytes > 0)
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wp.val + (size_t)b0 * 32),
+                   "r"(bytes * 2u)
+                   : "memory");
+  };
+
+  if (tid == 0) {
+    for (int i = 0; i < 3; ++i) mbar_init(&rb[i], 1);
+    for (int i = 0; i < 2; ++i) mbar_init(&wb[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int i = tid; i < 3 * KC * 32; i += blockDim.x) rows[(i >> 5) * RSW + N + (i & 31)] = 0.f;
+  for (int t = 0; t < K; ++t) {
+    const float* src = a.y_in + (size_t)a.clist[t] * N;
+    for (int j = tid; j < N; j += blockDim.x) rows[t * RSW + j] = src[j];
+  }
+  __syncthreads();
+  if (producer) {
+    load_bounds(a.first, s_gb[0]);
+    __syncwarp();
+    if (lane == 0) {
+      issue_weights(a.first, 0);
+      for (int d = 1; d < 4; ++d) prefetch_l2(a.first + d);
+    }
+  }
+  cluster.sync();  // every CTA's barriers exist before any remote store
+
+  uint32_t rpar = 0u, wpar = 0u;
+  for (int l = a.first; l < a.last; ++l) {
+    const int li = l - a.first;
+    const int cur = li % 3, nxt = (li + 1) % 3, wcur = li & 1;
+    const bool last = l + 1 == a.last;
+    if (li > 0) {
+      chain_wait(&rb[cur], (rpar >> cur) & 1u, failed, a.err);
+      rpar ^= 1u << cur;
+    }
+    if (producer) {
+      // inputs of layer l complete: the weight buffer of layer l - 1 is free
+      if (!last) {
+        load_bounds(l + 1, s_gb[wcur ^ 1]);
+        __syncwarp();
+        if (lane == 0) {
+          mbar_expect_tx(&rb[nxt], row_bytes);
+          issue_weights(l + 1, wcur ^ 1);
+          prefetch_l2(l + 4);
+        }
+      }
+      continue;
+    }
+    chain_wait(&wb[wcur], (wpar >> wcur) & 1u, failed, a.err);
+    wpar ^= 1u << wcur;
+    const LayerDev wl = s_wl[wcur];
+    const float* cur_rows = rows + (size_t)cur * KC * RSW;
+    const unsigned char* wsm = wbase + (size_t)wcur * a.wcap;
+    const int32_t gb0 = s_gb[wcur][0];
+    const int32_t nblk_all = s_gb[wcur][ng] - gb0;
+    const uint2* sidx = reinterpret_cast<const uint2*>(wsm);
+    const float4* sval = reinterpret_cast<const float4*>(wsm + (size_t)nblk_all * 32 * 8);
+    for (int g = gbeg + warp; g < gend; g += kChain2ComputeWarps) {
+      const int c = g * 32 + lane;
+      const float bc = wl.bias_vec ? __ldg(wl.bias_vec + c) : wl.bias;
+      const int32_t o = s_gb[wcur][g - gbeg] - gb0;
+      const int nb = s_gb[wcur][g - gbeg + 1] - s_gb[wcur][g - gbeg];
+      float acc[KC];
+#pragma unroll
+      for (int t = 0; t < KC; ++t) acc[t] = 0.f;
+      if (wl.val == nullptr)
+        accumulate_smem<KC, RSW, true>(acc, sidx + (size_t)o * 32, nullptr, nb, wl.wconst, cur_rows,
+                                       lane);
+      else
+        accumulate_smem<KC, RSW, false>(acc, sidx + (size_t)o * 32, sval + (size_t)o * 32, nb,
+                                        wl.wconst, cur_rows, lane);
+      const uint32_t nb_base = smem_u32(rows + (size_t)nxt * KC * RSW);
+#pragma unroll
+      for (int t = 0; t < KC; ++t) {
+        if (t < K) {
+          const float y = clampf(acc[t] + bc, a.clampv);
+          if (last) {
+            a.y_out[(size_t)a.clist[t] * N + c] = y;
+          } else {
+            const uint32_t la = nb_base + (uint32_t)(t * RSW + c) * 4u;
+            for (int p = 0; p < csize; ++p)
+              st_async_f32(mapa_u32(la, (uint32_t)p), y, mapa_u32(smem_u32(&rb[nxt]), (uint32_t)p));
+          }
+        }
+      }
+    }
+  }
+  if (producer && lane == 0 && *reinterpret_cast<volatile int32_t*>(a.err) != 0) {
+    // after a timeout the compute warps stop waiting: let the last copy issued
+    // into each buffer land before the CTA exits
+    for (int b = 0; b < 2; ++b) {
+      bool f2 = false;
+      if (wcnt[b] > 0) chain_wait(&wb[b], (uint32_t)(wcnt[b] - 1) & 1u, f2, a.err);
+    }
+  }
+  cluster.sync();  // no CTA leaves while another may still store into it
+}
+
+template __global__ void chain2_kernel<1056, 1>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 2>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 4>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 8>(const ChainArgs);
+template __global__ void chain2_kernel<4128, 1>(const ChainArgs);
+template __global__ void chain2_kernel<4128, 2>(const ChainArgs);
+
 template __global__ void chain_kernel<1056, 1>(const ChainArgs);
 template __global__ void chain_kernel<1056, 2>(const ChainArgs);
 template __global__ void chain_kernel<1056, 4>(const ChainArgs);
@@ -114,6 +334,29 @@ static const void* chain_fn(int rsw, int kc) {
   return nullptr;
 }
 
+static const void* chain2_fn(int rsw, int kc) {
+#define SDNN_PICK(R, K) \
+  if (rsw == R && kc == K) return (const void*)&chain2_kernel<R, K>;
+  SDNN_PICK(1056, 1)
+  SDNN_PICK(1056, 2)
+  SDNN_PICK(1056, 4)
+  SDNN_PICK(1056, 8)
+  SDNN_PICK(4128, 1)
+  SDNN_PICK(4128, 2)
+#undef SDNN_PICK
+  return nullptr;
+}
+
+uint32_t chain_slice_bytes(const int32_t* grp_blk, int G, bool general) {
+  uint32_t best = 0;
+  for (int r = 0; r < kChainCluster; ++r) {
+    const int gb = (int)((long)G * r / kChainCluster), ge = (int)((long)G * (r + 1) / kChainCluster);
+    const uint32_t nblk = (uint32_t)(grp_blk[ge] - grp_blk[gb]);
+    best = std::max(best, nblk * 32u * (general ? 24u : 8u));
+  }
+  return best;
+}
+
 int chain_capacity(int N) {
   const int rsw = N + 32;
   int best = 0;
@@ -122,22 +365,38 @@ int chain_capacity(int N) {
   return best;
 }
 
+static int chain_kc_for(int rsw, int kc_needed) {
+  for (int k : {1, 2, 4, 8})
+    if (k >= kc_needed && chain_fn(rsw, k)) return k;
+  return 0;
+}
+
+static size_t chain2_smem(int rsw, int kc, uint32_t wcap) {
+  return (size_t)3 * kc * rsw * sizeof(float) + (size_t)2 * wcap;
+}
+
+int chain_variant(const ChainArgs& a, int kc_needed) {
+  const int rsw = a.N + 32;
+  const int kc = chain_kc_for(rsw, kc_needed);
+  if (!kc) return 0;
+  if (a.wcap > 0 && a.G / kChainCluster <= kChain2MaxGroups && chain2_fn(rsw, kc) &&
+      chain2_smem(rsw, kc, a.wcap) <= 227 * 1024)
+    return 2;
+  return 1;
+}
+
 cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s) {
   const int rsw = a.N + 32;
-  int kc = 0;
-  for (int k : {1, 2, 4, 8})
-    if (k >= kc_needed && chain_fn(rsw, k)) {
-      kc = k;
-      break;
-    }
-  const void* fn = kc ? chain_fn(rsw, kc) : nullptr;
-  if (!fn) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)2 * kc * rsw * sizeof(float);
+  const int kc = chain_kc_for(rsw, kc_needed);
+  const int variant = chain_variant(a, kc_needed);
+  if (!variant) return cudaErrorInvalidValue;
+  const void* fn = variant == 2 ? chain2_fn(rsw, kc) : chain_fn(rsw, kc);
+  const size_t smem = variant == 2 ? chain2_smem(rsw, kc, a.wcap) : (size_t)2 * kc * rsw * sizeof(float);
   cudaError_t rc = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (rc != cudaSuccess) return rc;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kChainCluster);
-  cfg.blockDim = dim3(512);
+  cfg.blockDim = dim3(variant == 2 ? (kChain2ComputeWarps + 1) * 32 : 512);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];

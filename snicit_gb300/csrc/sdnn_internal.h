@@ -115,8 +115,16 @@ struct ChainArgs {
   const int32_t* ccount;
   int32_t N, G;
   float clampv;
+  int32_t* err;              // device error word (bounded waits)
+  uint32_t wcap;             // bytes of one streamed weight buffer (0 = no streaming)
 };
+// Bytes of the largest per-CTA weight slice of a layer for the chain kernels'
+// cluster split (grp_blk: G + 1 block offsets; general = per-edge values).
+uint32_t chain_slice_bytes(const int32_t* grp_blk, int G, bool general);
 int chain_capacity(int N);  // largest centroid count the chain kernel takes (0 = none)
+// Which chain kernel launch_chain would run: 0 none, 1 weights read from L2,
+// 2 weights streamed into shared memory.
+int chain_variant(const ChainArgs& a, int kc_needed);
 cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----

@@ -22,7 +22,7 @@ class Engine:
     def __init__(self, num_neurons=1024, num_layers=120, mode="SNICIT", threshold=30,
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
                  device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
-                 chain=True, merge=True, merge_start=0, merge_every=0):
+                 chain=True, merge=True, merge_start=0, merge_every=0, chain_stream=True):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -41,7 +41,8 @@ class Engine:
         cfg.flags = ((0 if binary_first_layer else _lib.FLAG_NO_BINARY_FIRST_LAYER)
                      | (0 if placement else _lib.FLAG_NO_PLACEMENT)
                      | (0 if chain else _lib.FLAG_NO_CHAIN)
-                | (0 if merge else _lib.FLAG_NO_MERGE))
+                | (0 if merge else _lib.FLAG_NO_MERGE)
+                | (0 if chain_stream else _lib.FLAG_NO_CHAIN_STREAM))
         cfg.merge_start = int(merge_start)
         cfg.merge_every = int(merge_every)
         self.cfg = cfg
@@ -154,7 +155,8 @@ class Engine:
             "tile_rows": s.tile_rows, "threads": s.threads,
             "pre_row_layers": s.pre_row_layers, "post_row_layers": s.post_row_layers,
             "weight_nnz": s.weight_nnz, "centroid_candidates": s.centroid_candidates,
-            "merge_start": s.merge_start,
+            "merge_start": s.merge_start, "merge_every": s.merge_every,
+            "post_kernel": s.post_kernel,
         }
 
     def layer_rows(self):

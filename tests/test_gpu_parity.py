@@ -299,7 +299,8 @@ def test_placement_gives_same_results(mode):
 
 
 @pytest.mark.parametrize("N,L,B,T,K", [(1024, 60, 600, 30, 50), (4096, 40, 200, 25, 8),
-                                       (1024, 30, 300, 2, 4)])
+                                       (1024, 30, 300, 2, 4), (4096, 60, 2000, 30, 50),
+                                       (16384, 36, 300, 30, 16)])
 def test_chain_path_is_bitwise_equal_to_per_layer_path(N, L, B, T, K):
     """When clustering leaves no residue row, the cluster chain kernel carries the
     centroid rows through the remaining layers; it must give the per-layer
@@ -309,15 +310,21 @@ def test_chain_path_is_bitwise_equal_to_per_layer_path(N, L, B, T, K):
     bias = sg.load().sdnn_reference_bias(N)
     Y0 = sg.generate_inputs(N, seed, 0, B)
     out = {}
-    for chain in (True, False):
+    for chain, stream in ((True, True), (True, False), (False, False)):
         with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=B, bias=bias, num_centroids=K,
-                       chain=chain) as eng:
+                       chain=chain, chain_stream=stream) as eng:
             eng.generate_weights(seed)
             flags, ids = eng.infer(Y0)
-            out[chain] = (flags, ids, eng.activations(B), eng.stats(), eng.layer_rows())
-    assert np.array_equal(out[True][1], out[False][1])
-    assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
-    assert np.array_equal(out[True][4], out[False][4])
+            out[chain, stream] = (flags, ids, eng.activations(B), eng.stats(), eng.layer_rows())
+    kinds = {k: v[3]["post_kernel"] for k, v in out.items()}
+    assert kinds[False, False] == 1
+    if kinds[True, False] != 1:  # the chain ran: streamed (3) and L2 (2) variants
+        assert kinds[True, False] == 2 and kinds[True, True] in (2, 3), kinds
+    for k in ((True, True), (True, False)):
+        assert np.array_equal(out[k][1], out[False, False][1])
+        assert np.array_equal(out[k][2].view(np.uint32), out[False, False][2].view(np.uint32)), k
+        assert np.array_equal(out[k][4], out[False, False][4])
+    out[True] = out[True, True]
     Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
     _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"chain N={N}", Y32=Y32)
 
