@@ -43,7 +43,7 @@ struct DevLayer {
   int64_t nnz = 0;
   int64_t slots = 0;
   int32_t max_depth = 0;
-  uint32_t chain_slice = 0;  // largest per-CTA weight slice for the chain kernels
+  uint32_t chain_slice8 = 0, chain_slice16 = 0;  // largest per-CTA weight slices (chain)
 };
 
 struct GraphKey {
@@ -143,7 +143,7 @@ struct sdnn_engine {
   int32_t* h_counts = nullptr;  // pinned: residue rows and centroids after clustering
   int chain_cap = 0;            // centroid rows the cluster chain kernel can carry
   int chain_kc = 1;
-  uint32_t chain_wcap = 0;      // streamed weight buffer of the chain kernel (bytes)
+  uint32_t chain_wcap8 = 0, chain_wcap16 = 0;  // chain kernel weight slices (bytes)
   bool last_chain = false;
   int last_post_kernel = 0;     // stats: 0 none, 1 per-layer launches, 2/3 chain kernel 1/2
   LayerDev* d_layer_table = nullptr;  // device copy of every layer's descriptor
@@ -284,7 +284,7 @@ int choose_kernel(sdnn_engine* e) {
   }
   for (const auto& k : cands) {
     if (req_T > 0 && k.T != req_T) continue;
-    const size_t smem = (size_t)layer_buffers(k.kg, k.rsw) * k.T * (size_t)(e->Q + 32) * 4;
+    const size_t smem = (size_t)k.T * (size_t)(e->Q + 32) * 4;
     if (smem > kMaxSmem) continue;
     if (!layer_instance_exists(k)) continue;
     LayerKernelKey kc = k, kg = k;
@@ -416,7 +416,10 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   d.nnz = p.nnz;
   d.slots = p.slots;
   d.max_depth = p.max_depth;
-  if (e->nq == 1) d.chain_slice = chain_slice_bytes(p.grp_blk.data(), e->G, !p.constw);
+  if (e->nq == 1) {
+    d.chain_slice8 = chain_slice_bytes(p.grp_blk.data(), e->G, !p.constw, 8);
+    d.chain_slice16 = chain_slice_bytes(p.grp_blk.data(), e->G, !p.constw, 16);
+  }
   cudaError_t rc = cudaSuccess;
   auto T = [&](cudaError_t r) {
     if (rc == cudaSuccess) rc = r;
@@ -544,8 +547,11 @@ int finalize_weights(sdnn_engine* e) {
     CK(cudaMemcpy(e->d_layer_table, table.data(), sizeof(LayerDev) * e->L, cudaMemcpyHostToDevice));
   }
   e->chain_cap = e->nq == 1 ? chain_capacity(e->N) : 0;
-  e->chain_wcap = 0;
-  for (const DevLayer& d : e->dl) e->chain_wcap = std::max(e->chain_wcap, d.chain_slice);
+  e->chain_wcap8 = e->chain_wcap16 = 0;
+  for (const DevLayer& d : e->dl) {
+    e->chain_wcap8 = std::max(e->chain_wcap8, d.chain_slice8);
+    e->chain_wcap16 = std::max(e->chain_wcap16, d.chain_slice16);
+  }
   if (!e->pos.empty()) {
     CK(cudaMalloc((void**)&e->d_perm_final, (size_t)e->N * 4));
     CK(cudaMemcpy(e->d_perm_final, e->pos[e->L - 1].data(), (size_t)e->N * 4,
@@ -776,7 +782,9 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
     ca.G = e->G;
     ca.clampv = e->cfg.clamp;
     ca.err = e->d_err;
-    ca.wcap = (e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM) ? 0u : e->chain_wcap;
+    ca.stream = !(e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM);
+    ca.wcap8 = e->chain_wcap8;
+    ca.wcap16 = e->chain_wcap16;
     CK(launch_chain(ca, e->chain_kc, s));
     e->launches++;
     if ((rc = record(e, 3, capturing))) return rc;
@@ -891,8 +899,10 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
       ChainArgs ca{};
       ca.N = e->N;
       ca.G = e->G;
-      ca.wcap = (e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM) ? 0u : e->chain_wcap;
-      e->last_post_kernel = 1 + chain_variant(ca, e->chain_kc);
+      ca.stream = !(e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM);
+      ca.wcap8 = e->chain_wcap8;
+      ca.wcap16 = e->chain_wcap16;
+      e->last_post_kernel = 1 + chain_plan(ca, e->chain_kc).variant;
     }
     if ((rc = run_phase(e, 4, PH_FINISH, rows, d_in, d_flags))) return rc;
   }

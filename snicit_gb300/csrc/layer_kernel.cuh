@@ -254,8 +254,8 @@ __device__ __forceinline__ void publish_rows(const LayerArgs& a, uint32_t m, int
 template <int T, int RSW, int KG, bool CONSTW>
 __global__ void __launch_bounds__(512) layer_kernel(const LayerArgs a) {
   extern __shared__ __align__(128) float ys[];
-  __shared__ __align__(8) uint64_t bar[2];
-  __shared__ int32_t s_rows[2][T];
+  __shared__ __align__(8) uint64_t bar[1];
+  __shared__ int32_t s_rows[1][T];
   __shared__ uint32_t s_mask;
   __shared__ int32_t s_fail;
 
@@ -263,14 +263,11 @@ __global__ void __launch_bounds__(512) layer_kernel(const LayerArgs a) {
   const int RS = RSW > 0 ? RSW : a.Q + 32;
   const Split sp = make_split<T>(a);
   if (sp.count <= 0 || (long)blockIdx.x >= sp.items) return;
-  // Whole-row layouts of N = 1024 / 4096: two tile buffers (the next tile
-  // streams in while this one is computed); otherwise one buffer, reloaded per
-  // item and input chunk.
-  constexpr int NBUF = layer_buffers(KG, RSW);
-  for (int i = tid; i < NBUF * T * 32; i += blockDim.x) ys[(i >> 5) * RS + a.Q + (i & 31)] = 0.f;
+  // One tile buffer, reloaded per item (and input chunk): the load of one CTA
+  // overlaps the compute of the other CTAs on the SM (up to four).
+  for (int i = tid; i < T * 32; i += blockDim.x) ys[(i >> 5) * RS + a.Q + (i & 31)] = 0.f;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
     s_mask = 0;
     s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -278,60 +275,7 @@ __global__ void __launch_bounds__(512) layer_kernel(const LayerArgs a) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
 
-  if constexpr (NBUF == 2) {
-    // item k of this CTA is blockIdx.x + k * gridDim.x; buffer k & 1
-    auto item_rows = [&](long item, int32_t* rows) -> int {
-      const int tile = (int)(item / sp.spl);
-      const int row0 = tile * T;
-      const int nrows = min(T, sp.count - row0);
-      for (int t = 0; t < T; ++t) rows[t] = t < nrows ? a.list_in[row0 + t] : -1;
-      return nrows;
-    };
-    if (tid == 0) {
-      for (int k = 0; k < 2; ++k) {
-        const long item = blockIdx.x + (long)k * gridDim.x;
-        if (item < sp.items) {
-          const int nr = item_rows(item, s_rows[k]);
-          load_tile(a, ys + (size_t)k * T * RS, RS, s_rows[k], nr, 0, &bar[k]);
-        }
-      }
-    }
-    uint32_t phases = 0u;  // bit b = parity to wait for on buffer b
-    int k = 0;
-    for (long item = blockIdx.x; item < sp.items; item += gridDim.x, ++k) {
-      const int buf = k & 1;
-      const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
-      const int nrows = min(T, sp.count - tile * T);
-      const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
-      const uint32_t parity = (phases >> buf) & 1u;
-      if (tid == 0) s_fail = mbar_wait_bounded(&bar[buf], parity, a.err) ? 0 : 1;
-      __syncthreads();
-      if (s_fail) return;
-      mbar_try_wait(&bar[buf], parity);
-      phases ^= 1u << buf;
-      const float* yb = ys + (size_t)buf * T * RS;
-      uint32_t m = 0;
-      for (int g = gbeg + warp; g < gend; g += nwarps) {
-        float acc[T];
-#pragma unroll
-        for (int t = 0; t < T; ++t) acc[t] = 0.f;
-        accumulate_group<T, RSW, CONSTW>(acc, a.w, a.nq, yb, RS, g, 0, lane);
-        m |= epilogue_group<T>(acc, a, s_rows[buf], nrows, g, lane);
-      }
-      if (lane == 0 && m) atomicOr(&s_mask, m);
-      __syncthreads();  // every warp is done with this buffer and its rows
-      if (tid == 0) {
-        const uint32_t mm = s_mask;
-        s_mask = 0;
-        publish_rows<T>(a, mm, tile, sp.spl, s_rows[buf]);
-        const long next = item + 2L * gridDim.x;
-        if (next < sp.items) {
-          const int nr = item_rows(next, s_rows[buf]);
-          load_tile(a, ys + (size_t)buf * T * RS, RS, s_rows[buf], nr, 0, &bar[buf]);
-        }
-      }
-    }
-  } else if constexpr (KG == 1) {
+  if constexpr (KG == 1) {
     // one buffer, whole rows (one chunk): reload per item, all groups of the part
     uint32_t phase = 0;
     int loaded_tile = -1;

@@ -93,22 +93,26 @@ __global__ void __launch_bounds__(512, 1) chain_kernel(const ChainArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// chain2_kernel: the same computation with the weights of the next layer
-// streamed into shared memory and point-to-point row exchange.
+// chain2_kernel: the same computation with the weights streamed into shared
+// memory and point-to-point row exchange.
 //
-//  * one producer warp (the last warp of the CTA) runs a layer ahead of the
-//    16 compute warps: as soon as the inputs of layer l are complete (so no
-//    warp still reads the weights of layer l - 1) it copies this CTA's slot
-//    blocks of layer l + 1 into the free one of two weight buffers with a 1-D
-//    TMA bulk copy (and the group offsets with plain loads), so the compute
-//    warps read indices from shared memory instead of waiting on L2;
+//  * one producer warp (the last warp of the CTA) copies this CTA's slot
+//    blocks of a layer into a shared weight buffer with a 1-D TMA bulk copy
+//    (and the group offsets with plain loads), so the 16 compute warps read
+//    indices from shared memory instead of waiting on L2.  With two weight
+//    buffers (NWBUF = 2) it runs a layer ahead: once the inputs of layer l are
+//    complete no warp reads the weights of layer l - 1 any more, and it
+//    fetches layer l + 1 into their buffer.  With one buffer (the weight slice
+//    of a layer is large: N = 16384) it fetches layer l + 1 as soon as the
+//    local compute warps are done with layer l;
 //  * outputs go to every CTA of the cluster with st.async, each signalling
 //    the receiving CTA's mbarrier for its next row buffer with 4 bytes; a CTA
 //    starts layer l + 1 when all N x K values of its next buffer have
 //    arrived -- no cluster-wide barrier per layer;
-//  * three row buffers: a CTA that has started layer l + 1 knows every CTA
-//    finished layer l - 1 (it received all of their layer-l outputs), so the
-//    buffer it writes for layer l + 2 is no longer read anywhere.
+//  * two row buffers suffice: a CTA that starts layer l has received every
+//    CTA's layer l - 1 outputs, which each CTA sends only after it has read
+//    all of its layer l - 1 inputs -- the buffer that layer l's outputs
+//    overwrite everywhere.
 // Same slots, same FMA order as layer_kernel and chain_kernel: bitwise equal.
 constexpr int kChain2ComputeWarps = 16;
 constexpr int kChain2MaxGroups = 64;  // groups per CTA (G / cluster size)
@@ -124,8 +128,11 @@ __device__ __forceinline__ void st_async_f32(uint32_t raddr, float v, uint32_t r
                "r"(__float_as_uint(v)), "r"(rbar)
                : "memory");
 }
-// Bounded wait shared by all threads; after a timeout (error word set) every
-// later wait of this thread is skipped so the kernel runs to its end.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait; after a timeout (error word set) every later wait of this
+// thread is skipped so the kernel runs to its end.
 __device__ __forceinline__ void chain_wait(uint64_t* bar, uint32_t parity, bool& failed,
                                            int32_t* err) {
   if (failed) return;
@@ -156,13 +163,14 @@ __device__ __forceinline__ void accumulate_smem(float (&acc)[KC], const uint2* _
   }
 }
 
-template <int RSW, int KC>
+template <int RSW, int KC, int NWBUF>
 __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kernel(const ChainArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
-  float* rows = reinterpret_cast<float*>(smem);  // [3][KC][RSW]
-  unsigned char* wbase = smem + (size_t)3 * KC * RSW * 4;  // [2][wcap]
-  __shared__ __align__(8) uint64_t rb[3];
-  __shared__ __align__(8) uint64_t wb[2];
+  float* rows = reinterpret_cast<float*>(smem);  // [2][KC][RSW]
+  unsigned char* wbase = smem + (size_t)2 * KC * RSW * 4;  // [NWBUF][wcap]
+  __shared__ __align__(8) uint64_t rb[2];  // row buffer b complete
+  __shared__ __align__(8) uint64_t wb[2];  // weight buffer b loaded
+  __shared__ __align__(8) uint64_t cd;     // local compute warps done with a layer (NWBUF = 1)
   __shared__ int32_t s_gb[2][kChain2MaxGroups + 1];
   __shared__ LayerDev s_wl[2];
   cg::cluster_group cluster = cg::this_cluster();
@@ -175,13 +183,14 @@ __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kern
   const int gbeg = (int)((long)a.G * rank / csize), gend = (int)((long)a.G * (rank + 1) / csize);
   const int ng = gend - gbeg;
   const uint32_t row_bytes = (uint32_t)K * (uint32_t)N * 4u;
+  const uint32_t wcap = a.wcap;
   bool failed = false;
+  int wcnt[2] = {0, 0};  // producer: copies issued into each weight buffer
 
   auto load_bounds = [&](int l, int32_t* dst) {  // producer warp
     const int32_t* gb = a.layers[l].grp_blk + gbeg;
     for (int i = lane; i <= ng; i += 32) dst[i] = __ldg(gb + i);
   };
-  int wcnt[2] = {0, 0};  // producer: copies issued into each weight buffer
   auto issue_weights = [&](int l, int buf) {  // producer lane 0, after load_bounds + syncwarp
     const LayerDev wl = a.layers[l];
     s_wl[buf] = wl;  // published to the compute warps by the arrive below
@@ -191,9 +200,15 @@ __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kern
     const uint32_t bv = wl.val ? (uint32_t)nblk * 32u * 16u : 0u;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&wb[buf], bi + bv);
-    unsigned char* dst = wbase + (size_t)buf * a.wcap;
+    unsigned char* dst = wbase + (size_t)buf * wcap;
     if (bi) bulk_g2s(dst, wl.idx + (size_t)b0 * 32, bi, &wb[buf]);
     if (bv) bulk_g2s(dst + bi, wl.val + (size_t)b0 * 32, bv, &wb[buf]);
+  };
+  auto fetch_layer = [&](int l, int buf) {  // whole producer warp
+    load_bounds(l, s_gb[buf]);
+    __syncwarp();
+    if (lane == 0) issue_weights(l, buf);
+    __syncwarp();
   };
   auto prefetch_l2 = [&](int l) {  // producer lane 0
     if (l >= a.last) return;
@@ -211,57 +226,69 @@ __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kern
   };
 
   if (tid == 0) {
-    for (int i = 0; i < 3; ++i) mbar_init(&rb[i], 1);
+    for (int i = 0; i < 2; ++i) mbar_init(&rb[i], 1);
     for (int i = 0; i < 2; ++i) mbar_init(&wb[i], 1);
+    mbar_init(&cd, kChain2ComputeWarps);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = tid; i < 3 * KC * 32; i += blockDim.x) rows[(i >> 5) * RSW + N + (i & 31)] = 0.f;
+  for (int i = tid; i < 2 * KC * 32; i += blockDim.x) rows[(i >> 5) * RSW + N + (i & 31)] = 0.f;
   for (int t = 0; t < K; ++t) {
     const float* src = a.y_in + (size_t)a.clist[t] * N;
     for (int j = tid; j < N; j += blockDim.x) rows[t * RSW + j] = src[j];
   }
   __syncthreads();
   if (producer) {
-    load_bounds(a.first, s_gb[0]);
-    __syncwarp();
-    if (lane == 0) {
-      issue_weights(a.first, 0);
+    fetch_layer(a.first, 0);
+    if (lane == 0)
       for (int d = 1; d < 4; ++d) prefetch_l2(a.first + d);
-    }
   }
   cluster.sync();  // every CTA's barriers exist before any remote store
 
-  uint32_t rpar = 0u, wpar = 0u;
+  uint32_t rpar = 0u, wpar = 0u, cdpar = 0u;
   for (int l = a.first; l < a.last; ++l) {
     const int li = l - a.first;
-    const int cur = li % 3, nxt = (li + 1) % 3, wcur = li & 1;
+    const int cur = li & 1, nxt = cur ^ 1;
+    const int wcur = NWBUF == 2 ? (li & 1) : 0;
     const bool last = l + 1 == a.last;
-    if (li > 0) {
-      chain_wait(&rb[cur], (rpar >> cur) & 1u, failed, a.err);
-      rpar ^= 1u << cur;
-    }
     if (producer) {
-      // inputs of layer l complete: the weight buffer of layer l - 1 is free
-      if (!last) {
-        load_bounds(l + 1, s_gb[wcur ^ 1]);
-        __syncwarp();
-        if (lane == 0) {
-          mbar_expect_tx(&rb[nxt], row_bytes);
-          issue_weights(l + 1, wcur ^ 1);
-          prefetch_l2(l + 4);
+      if constexpr (NWBUF == 2) {
+        // inputs of layer l complete: the weight buffer of layer l - 1 is free
+        if (li > 0) {
+          chain_wait(&rb[cur], (rpar >> cur) & 1u, failed, a.err);
+          rpar ^= 1u << cur;
+        }
+        if (!last) {
+          if (lane == 0) mbar_expect_tx(&rb[nxt], row_bytes);
+          fetch_layer(l + 1, wcur ^ 1);
+          if (lane == 0) prefetch_l2(l + 4);
+        }
+      } else {
+        // the single weight buffer: layer l was fetched when layer l - 1 was done
+        if (!last && lane == 0) mbar_expect_tx(&rb[nxt], row_bytes);
+        if (!last) {
+          chain_wait(&cd, cdpar, failed, a.err);
+          cdpar ^= 1u;
+          fetch_layer(l + 1, 0);
+          if (lane == 0) prefetch_l2(l + 3);
         }
       }
       continue;
+    }
+    if (li > 0) {
+      chain_wait(&rb[cur], (rpar >> cur) & 1u, failed, a.err);
+      rpar ^= 1u << cur;
     }
     chain_wait(&wb[wcur], (wpar >> wcur) & 1u, failed, a.err);
     wpar ^= 1u << wcur;
     const LayerDev wl = s_wl[wcur];
     const float* cur_rows = rows + (size_t)cur * KC * RSW;
-    const unsigned char* wsm = wbase + (size_t)wcur * a.wcap;
+    const unsigned char* wsm = wbase + (size_t)wcur * wcap;
     const int32_t gb0 = s_gb[wcur][0];
     const int32_t nblk_all = s_gb[wcur][ng] - gb0;
     const uint2* sidx = reinterpret_cast<const uint2*>(wsm);
     const float4* sval = reinterpret_cast<const float4*>(wsm + (size_t)nblk_all * 32 * 8);
+    const uint32_t nbuf_base = smem_u32(rows + (size_t)nxt * KC * RSW);
+    const uint32_t nbar = smem_u32(&rb[nxt]);
     for (int g = gbeg + warp; g < gend; g += kChain2ComputeWarps) {
       const int c = g * 32 + lane;
       const float bc = wl.bias_vec ? __ldg(wl.bias_vec + c) : wl.bias;
@@ -276,7 +303,6 @@ __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kern
       else
         accumulate_smem<KC, RSW, false>(acc, sidx + (size_t)o * 32, sval + (size_t)o * 32, nb,
                                         wl.wconst, cur_rows, lane);
-      const uint32_t nb_base = smem_u32(rows + (size_t)nxt * KC * RSW);
 #pragma unroll
       for (int t = 0; t < KC; ++t) {
         if (t < K) {
@@ -284,12 +310,16 @@ __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kern
           if (last) {
             a.y_out[(size_t)a.clist[t] * N + c] = y;
           } else {
-            const uint32_t la = nb_base + (uint32_t)(t * RSW + c) * 4u;
+            const uint32_t la = nbuf_base + (uint32_t)(t * RSW + c) * 4u;
             for (int p = 0; p < csize; ++p)
-              st_async_f32(mapa_u32(la, (uint32_t)p), y, mapa_u32(smem_u32(&rb[nxt]), (uint32_t)p));
+              st_async_f32(mapa_u32(la, (uint32_t)p), y, mapa_u32(nbar, (uint32_t)p));
           }
         }
       }
+    }
+    if constexpr (NWBUF == 1) {
+      __syncwarp();
+      if (lane == 0 && !last) mbar_arrive(&cd);
     }
   }
   if (producer && lane == 0 && *reinterpret_cast<volatile int32_t*>(a.err) != 0) {
@@ -303,12 +333,14 @@ __global__ void __launch_bounds__((kChain2ComputeWarps + 1) * 32, 1) chain2_kern
   cluster.sync();  // no CTA leaves while another may still store into it
 }
 
-template __global__ void chain2_kernel<1056, 1>(const ChainArgs);
-template __global__ void chain2_kernel<1056, 2>(const ChainArgs);
-template __global__ void chain2_kernel<1056, 4>(const ChainArgs);
-template __global__ void chain2_kernel<1056, 8>(const ChainArgs);
-template __global__ void chain2_kernel<4128, 1>(const ChainArgs);
-template __global__ void chain2_kernel<4128, 2>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 1, 2>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 2, 2>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 4, 2>(const ChainArgs);
+template __global__ void chain2_kernel<1056, 8, 2>(const ChainArgs);
+template __global__ void chain2_kernel<4128, 1, 2>(const ChainArgs);
+template __global__ void chain2_kernel<4128, 2, 2>(const ChainArgs);
+template __global__ void chain2_kernel<4128, 4, 2>(const ChainArgs);
+template __global__ void chain2_kernel<16416, 1, 1>(const ChainArgs);
 
 template __global__ void chain_kernel<1056, 1>(const ChainArgs);
 template __global__ void chain_kernel<1056, 2>(const ChainArgs);
@@ -334,23 +366,25 @@ static const void* chain_fn(int rsw, int kc) {
   return nullptr;
 }
 
-static const void* chain2_fn(int rsw, int kc) {
-#define SDNN_PICK(R, K) \
-  if (rsw == R && kc == K) return (const void*)&chain2_kernel<R, K>;
-  SDNN_PICK(1056, 1)
-  SDNN_PICK(1056, 2)
-  SDNN_PICK(1056, 4)
-  SDNN_PICK(1056, 8)
-  SDNN_PICK(4128, 1)
-  SDNN_PICK(4128, 2)
+static const void* chain2_fn(int rsw, int kc, int nwbuf) {
+#define SDNN_PICK(R, K, W) \
+  if (rsw == R && kc == K && nwbuf == W) return (const void*)&chain2_kernel<R, K, W>;
+  SDNN_PICK(1056, 1, 2)
+  SDNN_PICK(1056, 2, 2)
+  SDNN_PICK(1056, 4, 2)
+  SDNN_PICK(1056, 8, 2)
+  SDNN_PICK(4128, 1, 2)
+  SDNN_PICK(4128, 2, 2)
+  SDNN_PICK(4128, 4, 2)
+  SDNN_PICK(16416, 1, 1)
 #undef SDNN_PICK
   return nullptr;
 }
 
-uint32_t chain_slice_bytes(const int32_t* grp_blk, int G, bool general) {
+uint32_t chain_slice_bytes(const int32_t* grp_blk, int G, bool general, int cluster) {
   uint32_t best = 0;
-  for (int r = 0; r < kChainCluster; ++r) {
-    const int gb = (int)((long)G * r / kChainCluster), ge = (int)((long)G * (r + 1) / kChainCluster);
+  for (int r = 0; r < cluster; ++r) {
+    const int gb = (int)((long)G * r / cluster), ge = (int)((long)G * (r + 1) / cluster);
     const uint32_t nblk = (uint32_t)(grp_blk[ge] - grp_blk[gb]);
     best = std::max(best, nblk * 32u * (general ? 24u : 8u));
   }
@@ -371,42 +405,94 @@ static int chain_kc_for(int rsw, int kc_needed) {
   return 0;
 }
 
-static size_t chain2_smem(int rsw, int kc, uint32_t wcap) {
-  return (size_t)3 * kc * rsw * sizeof(float) + (size_t)2 * wcap;
+static size_t chain2_smem(int rsw, int kc, int nwbuf, uint32_t wcap) {
+  return (size_t)2 * kc * rsw * sizeof(float) + (size_t)nwbuf * wcap;
 }
 
-int chain_variant(const ChainArgs& a, int kc_needed) {
-  const int rsw = a.N + 32;
-  const int kc = chain_kc_for(rsw, kc_needed);
-  if (!kc) return 0;
-  if (a.wcap > 0 && a.G / kChainCluster <= kChain2MaxGroups && chain2_fn(rsw, kc) &&
-      chain2_smem(rsw, kc, a.wcap) <= 227 * 1024)
-    return 2;
-  return 1;
-}
-
-cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s) {
-  const int rsw = a.N + 32;
-  const int kc = chain_kc_for(rsw, kc_needed);
-  const int variant = chain_variant(a, kc_needed);
-  if (!variant) return cudaErrorInvalidValue;
-  const void* fn = variant == 2 ? chain2_fn(rsw, kc) : chain_fn(rsw, kc);
-  const size_t smem = variant == 2 ? chain2_smem(rsw, kc, a.wcap) : (size_t)2 * kc * rsw * sizeof(float);
-  cudaError_t rc = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (rc != cudaSuccess) return rc;
+// Whether a cluster of 16 CTAs (non-portable size) can run this kernel here.
+static bool cluster16_ok(const void* fn, int threads, size_t smem) {
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kChainCluster);
-  cfg.blockDim = dim3(variant == 2 ? (kChain2ComputeWarps + 1) * 32 : 512);
+  cfg.gridDim = dim3(16);
+  cfg.blockDim = dim3(threads);
   cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kChainCluster;
+  attr[0].val.clusterDim.x = 16;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  void* args[] = {const_cast<ChainArgs*>(&a)};
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n > 0;
+}
+
+ChainPlan chain_plan(const ChainArgs& a, int kc_needed) {
+  ChainPlan p{};
+  const int rsw = a.N + 32;
+  const int kc = chain_kc_for(rsw, kc_needed);
+  if (!kc) return p;
+  p.kc = kc;
+  p.variant = 1;
+  p.cluster = kChainCluster;
+  p.threads = 512;
+  p.smem = (size_t)2 * kc * rsw * sizeof(float);
+  if (!a.stream) return p;
+  const int threads2 = (kChain2ComputeWarps + 1) * 32;
+  // streamed weights: cluster 8 with two weight buffers, else 16 with two or one
+  const struct { int cluster, nwbuf; uint32_t wcap; } opts[] = {
+      {8, 2, a.wcap8}, {16, 2, a.wcap16}, {16, 1, a.wcap16}, {8, 1, a.wcap8}};
+  for (const auto& o : opts) {
+    if (o.wcap == 0 || (a.G + o.cluster - 1) / o.cluster > kChain2MaxGroups) continue;
+    const void* fn = chain2_fn(rsw, kc, o.nwbuf);
+    const size_t smem = chain2_smem(rsw, kc, o.nwbuf, o.wcap);
+    if (!fn || smem > 227 * 1024) continue;
+    if (o.cluster == 16 && !cluster16_ok(fn, threads2, smem)) continue;
+    p.variant = 2;
+    p.cluster = o.cluster;
+    p.nwbuf = o.nwbuf;
+    p.wcap = o.wcap;
+    p.threads = threads2;
+    p.smem = smem;
+    return p;
+  }
+  return p;
+}
+
+cudaError_t launch_chain(const ChainArgs& a0, int kc_needed, cudaStream_t s) {
+  const ChainPlan p = chain_plan(a0, kc_needed);
+  if (!p.variant) return cudaErrorInvalidValue;
+  const int rsw = a0.N + 32;
+  ChainArgs a = a0;
+  a.wcap = p.wcap;
+  const void* fn = p.variant == 2 ? chain2_fn(rsw, p.kc, p.nwbuf) : chain_fn(rsw, p.kc);
+  cudaError_t rc = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
+  if (rc != cudaSuccess) return rc;
+  if (p.cluster > 8) {
+    rc = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (rc != cudaSuccess) return rc;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p.cluster);
+  cfg.blockDim = dim3(p.threads);
+  cfg.dynamicSmemBytes = p.smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = p.cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  void* args[] = {&a};
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 

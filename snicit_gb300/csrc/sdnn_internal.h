@@ -58,11 +58,6 @@ struct LayerArgs {
 // instances with row stride chunk + 32 of these chunk sizes read them as such.
 inline bool slot_index_in_bytes(int Q) { return Q == 1024 || Q == 4096; }
 __host__ __device__ constexpr bool rsw_in_bytes(int rsw) { return rsw == 1056 || rsw == 4128; }
-// Tile buffers of a layer-kernel instance (2 = load of the next tile overlaps
-// the current one); the dynamic shared memory is buffers * T * (chunk + 32) * 4.
-__host__ __device__ constexpr int layer_buffers(int kg, int rsw) {
-  return (kg == 1 && rsw_in_bytes(rsw)) ? 2 : 1;
-}
 
 // Kernel instance selection.
 struct LayerKernelKey {
@@ -116,15 +111,22 @@ struct ChainArgs {
   int32_t N, G;
   float clampv;
   int32_t* err;              // device error word (bounded waits)
-  uint32_t wcap;             // bytes of one streamed weight buffer (0 = no streaming)
+  bool stream;               // weights may be streamed into shared memory
+  uint32_t wcap8, wcap16;    // largest per-CTA weight slice, clusters of 8 / 16 CTAs
+  uint32_t wcap;             // (set by launch_chain) bytes of one streamed weight buffer
 };
-// Bytes of the largest per-CTA weight slice of a layer for the chain kernels'
-// cluster split (grp_blk: G + 1 block offsets; general = per-edge values).
-uint32_t chain_slice_bytes(const int32_t* grp_blk, int G, bool general);
+// Bytes of the largest per-CTA weight slice of a layer when `cluster` CTAs
+// split its groups (grp_blk: G + 1 block offsets; general = per-edge values).
+uint32_t chain_slice_bytes(const int32_t* grp_blk, int G, bool general, int cluster);
 int chain_capacity(int N);  // largest centroid count the chain kernel takes (0 = none)
-// Which chain kernel launch_chain would run: 0 none, 1 weights read from L2,
-// 2 weights streamed into shared memory.
-int chain_variant(const ChainArgs& a, int kc_needed);
+// The chain launch for a centroid count: variant 0 none, 1 weights read from
+// L2, 2 weights streamed into shared memory (cluster size, weight buffers).
+struct ChainPlan {
+  int variant, kc, cluster, nwbuf, threads;
+  uint32_t wcap;
+  size_t smem;
+};
+ChainPlan chain_plan(const ChainArgs& a, int kc_needed);
 cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
