@@ -198,7 +198,8 @@ def run_ours(args):
 
     eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=B, bias=bias,
                     num_centroids=args.centroids, device=local, tile_rows=args.tile,
-                    threads=args.threads)
+                    threads=args.threads, merge_start=args.merge_start,
+                    merge_every=args.merge_every)
     eng.generate_weights(SEED, NNZ, 0.0625)
     t0 = time.perf_counter()
     eng.finalize()
@@ -524,6 +525,7 @@ CASES = {
     # name: (N, L, rows, mode, threshold) -- small fixed cases for ncu captures
     "plain-n4096": (4096, 6, 8192, "SNIG", 6),
     "chain-n4096": (4096, 60, 4096, "SNICIT", 30),
+    "plain-n65536": (65536, 3, 2048, "SNIG", 3),
 }
 
 
@@ -533,7 +535,8 @@ def run_case(args):
     N, L, B, mode, t = CASES[args.case]
     Y0 = sg.generate_inputs(N, SEED, 0, B)
     eng = sg.Engine(N, L, mode=mode, threshold=t, batch=B, bias=sg.load().sdnn_reference_bias(N),
-                    num_centroids=args.centroids, tile_rows=args.tile, threads=args.threads)
+                    num_centroids=args.centroids, tile_rows=args.tile, threads=args.threads,
+                    merge_start=args.merge_start, merge_every=args.merge_every)
     eng.generate_weights(SEED, NNZ, 0.0625)
     for _ in range(2):
         eng.infer(Y0)
@@ -554,6 +557,9 @@ def main():
     ap.add_argument("--tile", type=int, default=0, help="fix the layer-kernel tile rows (skips autotune)")
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--merge-start", type=int, default=0,
+                    help="first layer after which identical rows merge (0 = default/autotuned)")
+    ap.add_argument("--merge-every", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")

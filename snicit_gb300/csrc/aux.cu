@@ -186,16 +186,32 @@ __global__ void __launch_bounds__(1024) cand_select_kernel(ClusterArgs a) {
     atomicAdd(&hist[key >> 52], 1);
   }
   __syncthreads();
-  if (tid == 0) {
-    int cum = 0, cut = kHistBins - 1;
-    for (int b = 0; b < kHistBins; ++b) {
-      cum += hist[b];
-      if (cum >= K) {
-        cut = b;
-        break;
-      }
+  if (tid < 32) {
+    // first bin whose cumulative count reaches K: lane i sums bins
+    // [128 i, 128 i + 128), a warp scan finds the lane, that lane walks its bins
+    constexpr int per = kHistBins / 32;
+    int part = 0;
+    for (int b = 0; b < per; ++b) part += hist[tid * per + b];
+    int incl = part;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tid >= o) incl += v;
     }
-    s_cut = cut;
+    const unsigned hit = __ballot_sync(0xffffffffu, incl >= K);
+    if (hit == 0u) {
+      if (tid == 0) s_cut = kHistBins - 1;  // fewer live rows than K: all are candidates
+    } else if (tid == __ffs(hit) - 1) {
+      int cum = incl - part, cut = (tid + 1) * per - 1;
+      for (int b = 0; b < per; ++b) {
+        cum += hist[tid * per + b];
+        if (cum >= K) {
+          cut = tid * per + b;
+          break;
+        }
+      }
+      s_cut = cut;
+    }
   }
   __syncthreads();
   for (int i = tid; i < n; i += blockDim.x) {

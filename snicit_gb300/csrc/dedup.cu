@@ -62,8 +62,24 @@ __global__ void dedup_hash_kernel(const DedupArgs a) {
     const float* row = a.y + (size_t)r * a.N;
     uint32_t h1 = 0x243F6A88u, h2 = 0xB7E15162u;
     if (vec) {
+      // eight 16-byte loads in flight per lane, then the mixing (a few rows
+      // alone are otherwise one memory round trip per 512 bytes)
       const uint4* p = reinterpret_cast<const uint4*>(row);
-      for (int j = lane; j < (a.N >> 2); j += 32) {
+      const int n4 = a.N >> 2;
+      int j = lane;
+      for (; j + 7 * 32 < n4; j += 8 * 32) {
+        uint4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(p + j + k * 32);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          mix_in(h1, h2, v[k].x);
+          mix_in(h1, h2, v[k].y);
+          mix_in(h1, h2, v[k].z);
+          mix_in(h1, h2, v[k].w);
+        }
+      }
+      for (; j < n4; j += 32) {
         const uint4 v = __ldg(p + j);
         mix_in(h1, h2, v.x);
         mix_in(h1, h2, v.y);
@@ -113,7 +129,20 @@ __global__ void dedup_verify_kernel(const DedupArgs a) {
       if (vec) {
         const uint4* p = reinterpret_cast<const uint4*>(a.y + (size_t)r * a.N);
         const uint4* q = reinterpret_cast<const uint4*>(a.y + (size_t)rep * a.N);
-        for (int j = lane; j < (a.N >> 2); j += 32) {
+        const int n4 = a.N >> 2;
+        int j = lane;
+        for (; j + 3 * 32 < n4; j += 4 * 32) {
+          uint4 u[4], v[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            u[k] = __ldg(p + j + k * 32);
+            v[k] = __ldg(q + j + k * 32);
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            same &= u[k].x == v[k].x && u[k].y == v[k].y && u[k].z == v[k].z && u[k].w == v[k].w;
+        }
+        for (; j < n4; j += 32) {
           const uint4 u = __ldg(p + j), v = __ldg(q + j);
           same &= u.x == v.x && u.y == v.y && u.z == v.z && u.w == v.w;
         }

@@ -125,6 +125,8 @@ struct sdnn_engine {
   int32_t* d_rows = nullptr;      // row count of the current inference
   int32_t* d_fallback = nullptr;  // layer-0 rows of non-binary tiles
   int32_t* d_fbcount = nullptr;
+  uint32_t* d_bits = nullptr;      // chunked binary first layer: bit words per 32-row tile
+  int32_t* d_tile_state = nullptr;
   // merging of identical rows (SNICIT, below the threshold)
   int32_t* d_alias = nullptr;          // [cap] -1 or the row this row was merged into
   unsigned long long* d_mtable = nullptr;  // [mmask + 1]
@@ -134,6 +136,7 @@ struct sdnn_engine {
   int32_t* d_mcount = nullptr;         // [2]
   uint32_t mmask = 0;
   int bits_grid = 0;
+  bool bits_chunked = false;
 
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
@@ -219,6 +222,8 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_in);
   dfree(e->d_fallback);
   dfree(e->d_fbcount);
+  dfree(e->d_bits);
+  dfree(e->d_tile_state);
   dfree(e->d_rows);
   dfree(e->d_alias);
   dfree(e->d_mtable);
@@ -348,6 +353,11 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_ids, (size_t)cap * 4));
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
+  if (e->nq > 1 && layer0_bits_chunked_supported(e->N, e->Q)) {
+    const size_t tiles = (size_t)(cap + 31) / 32;
+    T(A(&e->d_bits, tiles * (size_t)N * 4));
+    T(A(&e->d_tile_state, tiles * 4));
+  }
   {
     uint64_t P = 1024;
     while (P < 2 * (uint64_t)cap) P <<= 1;
@@ -440,7 +450,12 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
     for (int c = 0; c < e->N; ++c) b[out_pos ? out_pos[c] : c] = e->hbias[l][c];
     T(cudaMemcpy(d.bias, b.data(), (size_t)e->N * 4, cudaMemcpyHostToDevice));
   }
-  if (rc == cudaSuccess && l == 0 && p.constw && p.max_depth < 128) {
+  int32_t max_in_degree = 0;  // counts of the binary first layer must fit 7 bits
+  if (l == 0 && p.constw) {
+    std::vector<int32_t> deg(e->N, 0);
+    for (int32_t c : h->cols) max_in_degree = std::max(max_in_degree, ++deg[c]);
+  }
+  if (rc == cudaSuccess && l == 0 && p.constw && p.max_depth < 128 && max_in_degree < 128) {
     // the float kernel adds w once per active edge: reproduce those sums
     float sums[128];
     float acc = 0.f;
@@ -669,7 +684,39 @@ int enqueue_plain_layers(sdnn_engine* e, int64_t rows, const float* d_in, int T,
       if ((rc = record(e, 2, capturing))) return rc;
     }
     const float* in = l == 0 ? d_in : e->d_y[(l - 1) & 1];
-    if (l == 0 && e->dl[0].sums && e->bits_grid > 0) {
+    if (l == 0 && e->dl[0].sums && e->bits_chunked) {
+      // binary inputs, input chunks: transpose pass + counting pass
+      CK(cudaMemsetAsync(e->d_fbcount, 0, 16, s));
+      Layer0Args b{};
+      b.idx = e->dl[0].idx;
+      b.grp_blk = e->dl[0].grp;
+      b.bias_vec = e->dl[0].bias;
+      b.bias = e->cfg.bias;
+      b.clampv = e->cfg.clamp;
+      b.sums = e->dl[0].sums;
+      b.y_in = in;
+      b.y_out = e->d_y[0];
+      b.list_in = e->d_list[0];
+      b.count_in = e->d_counts;
+      b.list_out = e->d_list[1];
+      b.count_out = e->d_counts + 1;
+      b.fallback_list = e->d_fallback;
+      b.fallback_count = e->d_fbcount;
+      b.N = e->N;
+      b.G = e->G;
+      b.nq = e->nq;
+      b.Q = e->Q;
+      b.bits = e->d_bits;
+      b.tile_state = e->d_tile_state;
+      b.tile_mask = e->d_tmask;
+      b.tile_ticket = e->d_ticket;
+      b.err = e->d_err;
+      CK(launch_layer0_bits_chunked(b, e->num_sms, s));
+      e->launches += 2;
+      if ((rc = layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount,
+                             e->d_list[1], e->d_counts + 1)))
+        return rc;
+    } else if (l == 0 && e->dl[0].sums && e->bits_grid > 0) {
       // binary inputs: counting kernel; tiles with other values go to the float kernel
       CK(cudaMemsetAsync(e->d_fbcount, 0, 16, s));
       Layer0Args b{};
@@ -935,6 +982,8 @@ int prepare(sdnn_engine* e, int64_t rows) {
   }
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, true}, e->smem));
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
+  e->bits_chunked = e->nq > 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
+                    layer0_bits_chunked_supported(e->N, e->Q);
   e->bits_grid = (e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
                   layer0_bits_supported(e->N))
                      ? layer0_bits_grid(e->N, e->num_sms, kBitsThreads)

@@ -20,6 +20,7 @@
 //
 // A tile holding any value other than 0 or 1 is not computed here: its rows
 // go to a fallback list that the float kernel processes right after.
+#include <algorithm>
 #include <cstdint>
 #include "layer_kernel.cuh"
 
@@ -164,6 +165,237 @@ __global__ void __launch_bounds__(512) layer0_bits_kernel(const Layer0Args a) {
       }
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Input chunks (N > 16384: a row of bit words does not fit shared memory).
+//
+// Pass 1, bits_transpose_kernel: one CTA per 32-row tile writes the tile's N
+// bit words to global memory (coalesced 16-byte stores) and flags tiles that
+// hold a value other than 0 or 1 (their rows go to the fallback list).
+// Pass 2, bits_count_chunked_kernel: an item is (tile, subset of groups); for
+// each input chunk the CTA copies the chunk's Q words into shared memory
+// (TMA bulk copy) and every warp adds the slots of its groups into bit-sliced
+// counters that stay in registers across the chunks; after the last chunk the
+// epilogue is the one of layer0_bits_kernel.  The rows that survive are
+// published per tile through the tile mask and ticket (the last subset of a
+// tile to finish appends them).
+constexpr int kChunkGroupsPerWarp = 4;
+constexpr int kChunkWarps = 16;
+
+__global__ void __launch_bounds__(256) bits_transpose_kernel(const Layer0Args a) {
+  __shared__ int32_t s_rows[32];
+  __shared__ int32_t s_nonbin;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int N = a.N;
+  const int count = *a.count_in;
+  const int n_tiles = (count + 31) / 32;
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int row0 = tile * 32;
+    const int nrows = min(32, count - row0);
+    __syncthreads();
+    if (tid < 32) s_rows[tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
+    if (tid == 0) s_nonbin = 0;
+    __syncthreads();
+    uint32_t* out = a.bits + (size_t)tile * N;
+    bool nonbin = false;
+    for (int j0 = warp * 128; j0 < N; j0 += nwarps * 128) {
+      const int j = j0 + lane * 4;
+      uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+      for (int t0 = 0; t0 < nrows; t0 += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (t0 + u < nrows)
+            v[u] = __ldg(reinterpret_cast<const float4*>(a.y_in + (size_t)s_rows[t0 + u] * N + j));
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (t0 + u < nrows) {
+            const float x[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) nonbin |= (x[q] != 0.f) && (x[q] != 1.f);
+            const uint32_t bit = 1u << (t0 + u);
+            w0 |= x[0] != 0.f ? bit : 0u;
+            w1 |= x[1] != 0.f ? bit : 0u;
+            w2 |= x[2] != 0.f ? bit : 0u;
+            w3 |= x[3] != 0.f ? bit : 0u;
+          }
+        }
+      }
+      *reinterpret_cast<uint4*>(out + j) = make_uint4(w0, w1, w2, w3);
+    }
+    if (__any_sync(0xffffffffu, nonbin) && lane == 0) s_nonbin = 1;
+    __syncthreads();
+    if (tid == 0) a.tile_state[tile] = s_nonbin;
+    if (s_nonbin && tid < nrows) {
+      const int pos = atomicAdd(a.fallback_count, 1);
+      a.fallback_list[pos] = s_rows[tid];
+    }
+  }
+}
+
+// Adds the slot words of nb blocks (indices ip, lane-strided) into bit-sliced
+// counters; the same carry-save tree as layer0_bits_kernel.
+__device__ __forceinline__ void count_blocks(uint32_t (&c)[7], const uint2* __restrict__ ip, int nb,
+                                             const uint32_t* bits) {
+  for (int b = 0; b < nb; b += 4) {
+    uint32_t w[16];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      uint2 iv = make_uint2(0u, 0u);
+      if (b + k < nb) iv = __ldg(ip + (size_t)(b + k) * 32);
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        const uint32_t word = s < 2 ? iv.x : iv.y;
+        const uint32_t j = (word >> ((s & 1) * 16)) & 0xffffu;
+        w[k * 4 + s] = (b + k < nb) ? bits[j] : 0u;
+      }
+    }
+    uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, c16;
+    csa(twosA, c[0], c[0], w[0], w[1]);
+    csa(twosB, c[0], c[0], w[2], w[3]);
+    csa(foursA, c[1], c[1], twosA, twosB);
+    csa(twosA, c[0], c[0], w[4], w[5]);
+    csa(twosB, c[0], c[0], w[6], w[7]);
+    csa(foursB, c[1], c[1], twosA, twosB);
+    csa(eightsA, c[2], c[2], foursA, foursB);
+    csa(twosA, c[0], c[0], w[8], w[9]);
+    csa(twosB, c[0], c[0], w[10], w[11]);
+    csa(foursA, c[1], c[1], twosA, twosB);
+    csa(twosA, c[0], c[0], w[12], w[13]);
+    csa(twosB, c[0], c[0], w[14], w[15]);
+    csa(foursB, c[1], c[1], twosA, twosB);
+    csa(eightsB, c[2], c[2], foursA, foursB);
+    csa(c16, c[3], c[3], eightsA, eightsB);
+    uint32_t cy = c16, t;
+    t = c[4] & cy; c[4] ^= cy; cy = t;
+    t = c[5] & cy; c[5] ^= cy; cy = t;
+    c[6] ^= cy;
+  }
+}
+
+__global__ void __launch_bounds__(kChunkWarps * 32) bits_count_chunked_kernel(const Layer0Args a) {
+  extern __shared__ __align__(128) uint32_t cbits[];  // Q + 32 words
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ float s_sum[128];
+  __shared__ int32_t s_rows[32];
+  __shared__ uint32_t s_mask;
+  __shared__ int32_t s_fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int N = a.N, Q = a.Q, nq = a.nq;
+  const int count = *a.count_in;
+  const int n_tiles = (count + 31) / 32;
+  constexpr int per_item = kChunkWarps * kChunkGroupsPerWarp;
+  const int subsets = (a.G + per_item - 1) / per_item;
+  const long items = (long)n_tiles * subsets;
+  if (tid < 128) s_sum[tid] = a.sums[tid];
+  for (int i = tid; i < 32; i += blockDim.x) cbits[Q + i] = 0u;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    s_mask = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  uint32_t phase = 0;
+  for (long item = blockIdx.x; item < items; item += gridDim.x) {
+    const int tile = (int)(item / subsets), sub = (int)(item % subsets);
+    const int row0 = tile * 32;
+    const int nrows = min(32, count - row0);
+    if (a.tile_state[tile]) continue;  // non-binary tile: the float kernel runs it
+    __syncthreads();
+    if (tid < 32) s_rows[tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
+    uint32_t c[kChunkGroupsPerWarp][7];
+#pragma unroll
+    for (int k = 0; k < kChunkGroupsPerWarp; ++k)
+#pragma unroll
+      for (int i = 0; i < 7; ++i) c[k][i] = 0u;
+    for (int q = 0; q < nq; ++q) {
+      __syncthreads();  // every warp is done with the previous chunk
+      if (tid == 0) {
+        const uint32_t bytes = (uint32_t)Q * 4u;
+        mbar_expect_tx(&bar, bytes);
+        const char* src = reinterpret_cast<const char*>(a.bits + (size_t)tile * N + (size_t)q * Q);
+        char* dst = reinterpret_cast<char*>(cbits);
+        for (uint32_t off = 0; off < bytes; off += 32768u)
+          bulk_g2s(dst + off, src + off, min(32768u, bytes - off), &bar);
+        s_fail = mbar_wait_bounded(&bar, phase, a.err) ? 0 : 1;
+      }
+      __syncthreads();
+      if (s_fail) return;
+      mbar_try_wait(&bar, phase);
+      phase ^= 1u;
+#pragma unroll
+      for (int k = 0; k < kChunkGroupsPerWarp; ++k) {
+        const int g = sub * per_item + k * kChunkWarps + warp;
+        if (g < a.G) {
+          const int32_t b0 = __ldg(a.grp_blk + g * nq + q), b1 = __ldg(a.grp_blk + g * nq + q + 1);
+          count_blocks(c[k], a.idx + (size_t)b0 * 32 + lane, b1 - b0, cbits);
+        }
+      }
+    }
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < kChunkGroupsPerWarp; ++k) {
+      const int g = sub * per_item + k * kChunkWarps + warp;
+      if (g >= a.G) continue;
+      const int c_out = g * 32 + lane;
+      const float bc = a.bias_vec ? __ldg(a.bias_vec + c_out) : a.bias;
+      for (int t = 0; t < nrows; ++t) {
+        uint32_t kk = 0;
+#pragma unroll
+        for (int i = 0; i < 7; ++i) kk |= ((c[k][i] >> t) & 1u) << i;
+        const float v = s_sum[kk] + bc;
+        a.y_out[(size_t)s_rows[t] * N + c_out] = clampf(v, a.clampv);
+        if (__any_sync(0xffffffffu, v > 0.f)) m |= 1u << t;
+      }
+    }
+    if (lane == 0 && m) atomicOr(&s_mask, m);
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t mm = s_mask;
+      s_mask = 0;
+      bool emit = true;
+      if (subsets > 1) {
+        atomicOr(a.tile_mask + tile, mm);
+        __threadfence();
+        const int tk = atomicAdd(a.tile_ticket + tile, 1);
+        emit = (tk == subsets - 1);
+        if (emit) {
+          __threadfence();
+          mm = atomicExch(a.tile_mask + tile, 0u);
+          a.tile_ticket[tile] = 0;
+        }
+      }
+      if (emit && mm) {
+        const int base = atomicAdd(a.count_out, __popc(mm));
+        int i = 0;
+        for (int t = 0; t < 32; ++t)
+          if (mm & (1u << t)) a.list_out[base + i++] = s_rows[t];
+      }
+    }
+  }
+}
+
+bool layer0_bits_chunked_supported(int N, int Q) {
+  return Q == 16384 && N % Q == 0 && N / Q > 1 && N % 128 == 0;
+}
+
+cudaError_t launch_layer0_bits_chunked(const Layer0Args& a, int num_sms, cudaStream_t s) {
+  if (!layer0_bits_chunked_supported(a.N, a.Q)) return cudaErrorInvalidValue;
+  bits_transpose_kernel<<<num_sms * 4, 256, 0, s>>>(a);
+  cudaError_t rc = cudaGetLastError();
+  if (rc != cudaSuccess) return rc;
+  const void* fn = (const void*)&bits_count_chunked_kernel;
+  const size_t smem = (size_t)(a.Q + 32) * 4;
+  rc = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (rc != cudaSuccess) return rc;
+  int per_sm = 0;
+  rc = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kChunkWarps * 32, smem);
+  if (rc != cudaSuccess) return rc;
+  void* args[] = {const_cast<Layer0Args*>(&a)};
+  return cudaLaunchKernel(fn, dim3(num_sms * std::max(1, per_sm)), dim3(kChunkWarps * 32), args,
+                          smem, s);
 }
 
 template __global__ void layer0_bits_kernel<1056>(const Layer0Args);

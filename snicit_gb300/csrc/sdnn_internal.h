@@ -94,10 +94,22 @@ struct Layer0Args {
   int32_t* fallback_list;    // rows of tiles with non-binary inputs
   int32_t* fallback_count;
   int32_t N, G;
+  // input chunks (N > 16384): bit words staged in global memory per tile
+  int32_t nq, Q;
+  uint32_t* bits;            // [tiles][N] words (bit t = input of row t of the tile)
+  int32_t* tile_state;       // [tiles]: 1 = tile holds non-binary values
+  uint32_t* tile_mask;       // scratch per tile, zero between launches
+  int32_t* tile_ticket;      // scratch per tile, zero between launches
+  int32_t* err;              // device error word (bounded waits)
 };
 bool layer0_bits_supported(int N);
 int layer0_bits_grid(int N, int num_sms, int threads);
 cudaError_t launch_layer0_bits(const Layer0Args& a, int grid, int threads, cudaStream_t s);
+// Chunked variant (nq > 1, chunks of Q = 16384): a transpose pass writes each
+// 32-row tile's bit words to `bits`, then the counting pass keeps bit-sliced
+// counters of a subset of groups in registers across the chunks.
+bool layer0_bits_chunked_supported(int N, int Q);
+cudaError_t launch_layer0_bits_chunked(const Layer0Args& a, int num_sms, cudaStream_t s);
 
 // Post-threshold layers with no residue rows left (post_chain.cu): one
 // cluster carries the K centroid rows through layers [first, last).

@@ -260,7 +260,8 @@ def test_autotune_keeps_categories():
     assert np.array_equal(ids, np.flatnonzero(alive))
 
 
-@pytest.mark.parametrize("N,L,B", [(1024, 8, 700), (4096, 5, 300), (16384, 3, 70)])
+@pytest.mark.parametrize("N,L,B", [(1024, 8, 700), (4096, 5, 300), (16384, 3, 70),
+                                   (65536, 2, 100)])
 def test_binary_first_layer_is_bitwise_equal(N, L, B):
     """The counting first-layer kernel gives the float kernel's bits exactly;
     tiles with a non-binary value fall back to the float kernel."""
@@ -273,7 +274,8 @@ def test_binary_first_layer_is_bitwise_equal(N, L, B):
                        binary_first_layer=fast) as eng:
             eng.generate_weights(seed)
             flags, ids = eng.infer(Y0)
-            out[fast] = (flags, ids, eng.activations(B))
+            out[fast] = (flags, ids, eng.activations(B), eng.stats())
+    assert out[True][3]["launches"] > out[False][3]["launches"], "counting kernel not used"
     assert np.array_equal(out[True][1], out[False][1])
     assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
     Yref, alive, Y32 = _ref(_layers(N, L, seed), N, sg.load().sdnn_reference_bias(N), Y0)
