@@ -93,6 +93,8 @@ typedef struct sdnn_config {
                                            /* activations agree within FP32 rounding)       */
 #define SDNN_FLAG_NO_CHAIN_STREAM 16       /* chain kernel reads weights from L2 instead  */
                                            /* of streaming them into shared memory        */
+#define SDNN_FLAG_NO_GRID_CHAIN 32         /* no grid-wide chain: the cluster chain (or    */
+                                           /* per-layer launches where it cannot run)     */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -116,8 +118,9 @@ typedef struct sdnn_stats {
   int32_t merge_start;   /* first layer after which identical rows are merged     */
   int32_t merge_every;   /* ... and the spacing of the following merge steps      */
   int32_t post_kernel;   /* post-threshold path: 0 none, 1 a centroid and a residue
-                            launch per layer, 2 chain kernel (weights from L2),
-                            3 chain kernel (weights streamed to shared memory)    */
+                            launch per layer, 2 cluster chain kernel (weights from
+                            L2), 3 cluster chain kernel (weights streamed to shared
+                            memory), 4 grid-wide chain kernel                     */
 } sdnn_stats;
 
 typedef struct sdnn_engine sdnn_engine;

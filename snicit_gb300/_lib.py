@@ -15,6 +15,7 @@ FLAG_NO_PLACEMENT = 2
 FLAG_NO_CHAIN = 4
 FLAG_NO_MERGE = 8
 FLAG_NO_CHAIN_STREAM = 16
+FLAG_NO_GRID_CHAIN = 32
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",

@@ -56,7 +56,7 @@ struct LayerArgs {
 // Chunk sizes whose packed slot indices are byte offsets into the shared row
 // (u16 holds (chunk + 32) * 4 only for chunks up to 16351 floats); the kernel
 // instances with row stride chunk + 32 of these chunk sizes read them as such.
-inline bool slot_index_in_bytes(int Q) { return Q == 1024 || Q == 4096; }
+__host__ __device__ inline bool slot_index_in_bytes(int Q) { return Q == 1024 || Q == 4096; }
 __host__ __device__ constexpr bool rsw_in_bytes(int rsw) { return rsw == 1056 || rsw == 4128; }
 
 // Kernel instance selection.
@@ -140,6 +140,25 @@ struct ChainPlan {
 };
 ChainPlan chain_plan(const ChainArgs& a, int kc_needed);
 cudaError_t launch_chain(const ChainArgs& a, int kc_needed, cudaStream_t s);
+
+// The same for any width, as one cooperative launch over the GPU with the
+// rows in global scratch (post_grid.cu).
+struct GridChainArgs {
+  const LayerDev* layers;    // [L] device table
+  int32_t first, last;
+  const float* y_in;         // activations at the threshold
+  float* y_out;              // final buffer
+  const int32_t* clist;
+  const int32_t* ccount;
+  int32_t N, G, nq, Q;
+  float clampv;
+  float* scratch;            // [layers + 1][8][nq][Q + 32]: one buffer per layer
+  unsigned int* barrier;     // grid barrier counter (zeroed by the launch)
+  int32_t* err;
+};
+int grid_chain_capacity();
+size_t grid_chain_scratch_floats(int layers, int nq, int Q);
+cudaError_t launch_grid_chain(const GridChainArgs& a, int kc_needed, int num_sms, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);

@@ -22,7 +22,8 @@ class Engine:
     def __init__(self, num_neurons=1024, num_layers=120, mode="SNICIT", threshold=30,
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
                  device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
-                 chain=True, merge=True, merge_start=0, merge_every=0, chain_stream=True):
+                 chain=True, merge=True, merge_start=0, merge_every=0, chain_stream=True,
+                 grid_chain=True):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -42,7 +43,8 @@ class Engine:
                      | (0 if placement else _lib.FLAG_NO_PLACEMENT)
                      | (0 if chain else _lib.FLAG_NO_CHAIN)
                 | (0 if merge else _lib.FLAG_NO_MERGE)
-                | (0 if chain_stream else _lib.FLAG_NO_CHAIN_STREAM))
+                | (0 if chain_stream else _lib.FLAG_NO_CHAIN_STREAM)
+                | (0 if grid_chain else _lib.FLAG_NO_GRID_CHAIN))
         cfg.merge_start = int(merge_start)
         cfg.merge_every = int(merge_every)
         self.cfg = cfg

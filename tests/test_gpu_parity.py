@@ -302,33 +302,38 @@ def test_placement_gives_same_results(mode):
 
 @pytest.mark.parametrize("N,L,B,T,K", [(1024, 60, 600, 30, 50), (4096, 40, 200, 25, 8),
                                        (1024, 30, 300, 2, 4), (4096, 60, 2000, 30, 50),
-                                       (16384, 36, 300, 30, 16)])
+                                       (16384, 36, 300, 30, 16), (65536, 33, 160, 30, 8)])
 def test_chain_path_is_bitwise_equal_to_per_layer_path(N, L, B, T, K):
-    """When clustering leaves no residue row, the cluster chain kernel carries the
-    centroid rows through the remaining layers; it must give the per-layer
-    launches' bits.  (With early thresholds residues remain and both runs take
-    the per-layer path.)"""
+    """When clustering leaves no residue row, one chain launch carries the
+    centroid rows through the remaining layers (cluster kernel with streamed
+    weights, cluster kernel reading L2, or the grid-wide kernel); each must give
+    the per-layer launches' bits.  (With early thresholds residues remain and
+    every run takes the per-layer path.)"""
     seed = 400 + N + T
     bias = sg.load().sdnn_reference_bias(N)
     Y0 = sg.generate_inputs(N, seed, 0, B)
+    runs = {"layers": dict(chain=False), "default": dict(),
+            "cluster_l2": dict(chain_stream=False, grid_chain=False),
+            "grid": dict(chain_stream=False, chain=True)}
     out = {}
-    for chain, stream in ((True, True), (True, False), (False, False)):
+    for name, kw in runs.items():
         with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=B, bias=bias, num_centroids=K,
-                       chain=chain, chain_stream=stream) as eng:
+                       **kw) as eng:
             eng.generate_weights(seed)
             flags, ids = eng.infer(Y0)
-            out[chain, stream] = (flags, ids, eng.activations(B), eng.stats(), eng.layer_rows())
+            out[name] = (flags, ids, eng.activations(B), eng.stats(), eng.layer_rows())
     kinds = {k: v[3]["post_kernel"] for k, v in out.items()}
-    assert kinds[False, False] == 1
-    if kinds[True, False] != 1:  # the chain ran: streamed (3) and L2 (2) variants
-        assert kinds[True, False] == 2 and kinds[True, True] in (2, 3), kinds
-    for k in ((True, True), (True, False)):
-        assert np.array_equal(out[k][1], out[False, False][1])
-        assert np.array_equal(out[k][2].view(np.uint32), out[False, False][2].view(np.uint32)), k
-        assert np.array_equal(out[k][4], out[False, False][4])
-    out[True] = out[True, True]
+    assert kinds["layers"] == 1
+    if out["layers"][3]["residue_rows"] == 0 and out["layers"][3]["centroids"] > 0:
+        assert kinds["grid"] in (2, 3, 4), kinds  # a chain kernel of some kind
+        assert kinds["cluster_l2"] in (1, 2), kinds
+    for k in ("default", "cluster_l2", "grid"):
+        assert np.array_equal(out[k][1], out["layers"][1])
+        assert np.array_equal(out[k][2].view(np.uint32), out["layers"][2].view(np.uint32)), (k, kinds)
+        assert np.array_equal(out[k][4], out["layers"][4])
     Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
-    _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"chain N={N}", Y32=Y32)
+    _check(out["default"][2], out["default"][0], out["default"][1], Yref, alive,
+           f"chain N={N}", Y32=Y32)
 
 
 @pytest.mark.parametrize("mode", ["SNIG", "SNICIT"])
