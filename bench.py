@@ -172,6 +172,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def load_weights(eng, args, N, L):
+    """Seeded weights, packed on the host and uploaded -- or, with
+    --weights-cache DIR, taken from DIR's packed-weight file (written on the
+    first run).  Returns where they came from."""
+    path = None
+    if args.weights_cache:
+        os.makedirs(args.weights_cache, exist_ok=True)
+        path = os.path.join(args.weights_cache, f"sdgc-{N}x{L}-seed{SEED}.sdnnw")
+        if os.path.exists(path):
+            eng.load_packed(path)
+            eng.finalize()
+            return "packed file (mmap)"
+    eng.generate_weights(SEED, NNZ, 0.0625)
+    eng.finalize()
+    if path:
+        eng.save_packed(path)
+    return "generated + packed"
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -200,9 +219,8 @@ def run_ours(args):
                     num_centroids=args.centroids, device=local, tile_rows=args.tile,
                     threads=args.threads, merge_start=args.merge_start,
                     merge_every=args.merge_every)
-    eng.generate_weights(SEED, NNZ, 0.0625)
     t0 = time.perf_counter()
-    eng.finalize()
+    weights = load_weights(eng, args, N, L)
     pack_s = time.perf_counter() - t0
     if not args.no_autotune and not args.tile:
         rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
@@ -345,7 +363,7 @@ def run_ours(args):
             "p99_ms": sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))],
             "survivors": int(flags.sum()),
             "stage_ms": st["stage_ms"],
-            "pack_s": pack_s,
+            "pack_s": pack_s, "weights": weights,
             "plain": {"ms_per_inference": plain_ms, "edges_per_s": edges / (plain_ms / 1e3),
                       "category_set_equal": plain_exact, "row_layers": pst["row_layers"]},
             "speedup_vs_plain": plain_ms / ms_per_step,
@@ -560,6 +578,8 @@ def main():
     ap.add_argument("--merge-start", type=int, default=0,
                     help="first layer after which identical rows merge (0 = default/autotuned)")
     ap.add_argument("--merge-every", type=int, default=0)
+    ap.add_argument("--weights-cache", default=None,
+                    help="directory of packed-weight files (written on the first run)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")

@@ -217,6 +217,15 @@ int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows);
 /* Statistics of the last inference. */
 int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
 
+/* Packed-weight files: the packed slot layout and neuron placement of every
+ * layer, written once (packing runs on the host, no GPU needed) and loaded
+ * with one mmap by later engines of the same N and L, which then skip the
+ * packing (seconds per thousand layers at N = 65536).  The reference caches
+ * its XY preprocessing the same way (src/SDGC/SNICIT/SNICIT.hpp:127-182).
+ * Loading validates every slot index and the placement before upload. */
+int sdnn_save_packed_weights(sdnn_engine* e, const char* path);
+int sdnn_load_packed_weights(sdnn_engine* e, const char* path);
+
 /* Switches the mode (and threshold) of an engine without repacking its
  * weights, e.g. to time the plain path and SNICIT on one resident copy of W.
  * (The reference picks the engine class once, main/SDGC.cu:104-110.) */
@@ -325,6 +334,16 @@ int sdnn_generate_inputs_device(int32_t num_neurons, uint64_t seed, int64_t row_
 int sdnn_generate_layer_coo(int32_t num_neurons, uint64_t seed, int32_t layer,
                             int32_t nnz_per_row, float value, int32_t* rows,
                             int32_t* cols, float* vals);
+
+/* Binary input files (no reference counterpart; they replace parsing the
+ * input TSV, src/SDGC/utility.hpp:160-191): encoding 0 = FP32 rows, 1 = one
+ * bit per entry (0/1 inputs only; SDNN_ERR_INVALID otherwise).  Reads map
+ * the file and decode any row window. */
+int sdnn_write_inputs_bin(const char* path, const float* Y0, int64_t rows, int32_t num_neurons,
+                          int32_t encoding);
+int sdnn_inputs_bin_info(const char* path, int32_t* num_neurons, int64_t* rows, int32_t* encoding);
+int sdnn_read_inputs_bin(const char* path, int32_t num_neurons, int64_t row_offset, int64_t rows,
+                         float* out);
 
 /* Writers for the reference formats: weights dir/n{N}-l{l}.tsv, inputs
  * sparse-images-{N}.tsv, categories one 1-based id per line. */

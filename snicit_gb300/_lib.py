@@ -101,6 +101,8 @@ SIGNATURES = [
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_autotune_device", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_set_mode", ctypes.c_int, [P, I32, I32]),
+    ("sdnn_save_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
+    ("sdnn_load_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_layer_noalloc", ctypes.c_int, [P, I32, P, P, I64, P, P]),
     ("sdnn_server_config_default", ctypes.c_int, [P]),
     ("sdnn_server_create", ctypes.c_int, [P, P, P, P, P]),
@@ -116,6 +118,9 @@ SIGNATURES = [
     ("sdnn_write_weights_tsv", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_write_inputs_tsv", ctypes.c_int, [ctypes.c_char_p, P, I64, I32]),
     ("sdnn_write_categories_tsv", ctypes.c_int, [ctypes.c_char_p, P, I64]),
+    ("sdnn_write_inputs_bin", ctypes.c_int, [ctypes.c_char_p, P, I64, I32, I32]),
+    ("sdnn_inputs_bin_info", ctypes.c_int, [ctypes.c_char_p, P, P, P]),
+    ("sdnn_read_inputs_bin", ctypes.c_int, [ctypes.c_char_p, I32, I64, I64, P]),
 ]
 
 _lib = None

@@ -18,6 +18,7 @@
 
 #include <cuda_runtime.h>
 
+#include "packfile.h"
 #include "sdnn_internal.h"
 #include "snicit_gb300.h"
 #include "wpack.h"
@@ -82,6 +83,7 @@ struct sdnn_engine {
   std::vector<HostLayer> hw;
   std::vector<std::vector<float>> hbias;
   GenSpec gen;
+  std::shared_ptr<PackedFile> packed;  // weights from a packed-weight file
   bool weights_dirty = true;
 
   // kernel configuration
@@ -413,8 +415,9 @@ const HostLayer* host_layer(sdnn_engine* e, int l, HostLayer& tmp) {
   return &tmp;
 }
 
-// Packs layer l with the chosen neuron placement and uploads it.
-int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
+// Packs layer l on the host with the chosen neuron placement (e->pos).
+int pack_host_layer(sdnn_engine* e, int l, PackedLayer& p, int32_t& max_in_degree,
+                    std::string& err) {
   HostLayer tmp;
   const HostLayer* h = host_layer(e, l, tmp);
   if (!h) {
@@ -423,11 +426,62 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   }
   const int32_t* in_pos = (l > 0 && !e->pos.empty()) ? e->pos[l - 1].data() : nullptr;
   const int32_t* out_pos = e->pos.empty() ? nullptr : e->pos[l].data();
-  PackedLayer p;
   if (!pack_layer_placed(*h, e->N, e->Q, slot_index_in_bytes(e->Q) ? 4 : 1, in_pos, out_pos, p)) {
     err = "bad chunk size for packing";
     return SDNN_ERR_INVALID;
   }
+  max_in_degree = 0;  // counts of the binary first layer must fit 7 bits
+  if (p.constw) {
+    std::vector<int32_t> deg(e->N, 0);
+    for (int32_t c : h->cols) max_in_degree = std::max(max_in_degree, ++deg[c]);
+  }
+  return SDNN_OK;
+}
+
+PackedView view_of(const sdnn_engine* e, int l, const PackedLayer& p, int32_t max_in_degree) {
+  PackedView v;
+  v.grp_blk = p.grp_blk.data();
+  v.idx = p.idx.data();
+  v.val = p.constw ? nullptr : p.val.data();
+  v.bias = l < (int)e->hbias.size() && !e->hbias[l].empty() ? e->hbias[l].data() : nullptr;
+  v.pos = e->pos.empty() ? nullptr : e->pos[l].data();
+  v.constw = p.constw;
+  v.wconst = p.wconst;
+  v.nblocks = p.nblocks;
+  v.nnz = p.nnz;
+  v.slots = p.slots;
+  v.max_depth = p.max_depth;
+  v.max_in_degree = max_in_degree;
+  return v;
+}
+
+// Checks a packed layer from a file before it reaches the GPU: every slot
+// index inside the shared row (chunk + 32 zero floats), positions in range.
+bool check_view(const sdnn_engine* e, const PackedView& v, std::string& err) {
+  const uint32_t limit = (uint32_t)(e->Q + 32) * (slot_index_in_bytes(e->Q) ? 4u : 1u);
+  const size_t n = (size_t)v.nblocks * 128;
+  const uint32_t step = slot_index_in_bytes(e->Q) ? 4u : 1u;
+  for (size_t i = 0; i < n; ++i)
+    if (v.idx[i] >= limit || v.idx[i] % step != 0) {
+      err = "slot index out of range";
+      return false;
+    }
+  if (v.pos) {
+    std::vector<char> seen(e->N, 0);
+    for (int c = 0; c < e->N; ++c) {
+      const int32_t q = v.pos[c];
+      if (q < 0 || q >= e->N || seen[q]) {
+        err = "placement is not a permutation";
+        return false;
+      }
+      seen[q] = 1;
+    }
+  }
+  return true;
+}
+
+// Uploads one packed layer (slots, offsets, values, placed bias, first-layer sums).
+int upload_layer(sdnn_engine* e, int l, const PackedView& p, std::string& err) {
   DevLayer d;
   d.constw = p.constw;
   d.wconst = p.wconst;
@@ -435,35 +489,30 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
   d.slots = p.slots;
   d.max_depth = p.max_depth;
   if (e->nq == 1) {
-    d.chain_slice8 = chain_slice_bytes(p.grp_blk.data(), e->G, !p.constw, 8);
-    d.chain_slice16 = chain_slice_bytes(p.grp_blk.data(), e->G, !p.constw, 16);
+    d.chain_slice8 = chain_slice_bytes(p.grp_blk, e->G, !p.constw, 8);
+    d.chain_slice16 = chain_slice_bytes(p.grp_blk, e->G, !p.constw, 16);
   }
+  const size_t nslot = (size_t)p.nblocks * 128;
+  const size_t ngrp = (size_t)e->G * e->nq + 1;
   cudaError_t rc = cudaSuccess;
   auto T = [&](cudaError_t r) {
     if (rc == cudaSuccess) rc = r;
   };
-  T(cudaMalloc((void**)&d.idx, std::max<size_t>(p.idx.size() * 2, 16)));
-  T(cudaMalloc((void**)&d.grp, p.grp_blk.size() * 4));
-  if (!p.constw) T(cudaMalloc((void**)&d.val, std::max<size_t>(p.val.size() * 4, 16)));
-  const bool has_bias = l < (int)e->hbias.size() && !e->hbias[l].empty();
-  if (has_bias) T(cudaMalloc((void**)&d.bias, (size_t)e->N * 4));
-  if (rc == cudaSuccess && !p.idx.empty())
-    T(cudaMemcpy(d.idx, p.idx.data(), p.idx.size() * 2, cudaMemcpyHostToDevice));
-  if (rc == cudaSuccess) T(cudaMemcpy(d.grp, p.grp_blk.data(), p.grp_blk.size() * 4, cudaMemcpyHostToDevice));
-  if (rc == cudaSuccess && d.val && !p.val.empty())
-    T(cudaMemcpy(d.val, p.val.data(), p.val.size() * 4, cudaMemcpyHostToDevice));
-  if (rc == cudaSuccess && has_bias) {
+  T(cudaMalloc((void**)&d.idx, std::max<size_t>(nslot * 2, 16)));
+  T(cudaMalloc((void**)&d.grp, ngrp * 4));
+  if (!p.constw) T(cudaMalloc((void**)&d.val, std::max<size_t>(nslot * 4, 16)));
+  if (p.bias) T(cudaMalloc((void**)&d.bias, (size_t)e->N * 4));
+  if (rc == cudaSuccess && nslot) T(cudaMemcpy(d.idx, p.idx, nslot * 2, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess) T(cudaMemcpy(d.grp, p.grp_blk, ngrp * 4, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess && d.val && nslot)
+    T(cudaMemcpy(d.val, p.val, nslot * 4, cudaMemcpyHostToDevice));
+  if (rc == cudaSuccess && p.bias) {
     // per-neuron bias follows its neuron to its position
     std::vector<float> b(e->N);
-    for (int c = 0; c < e->N; ++c) b[out_pos ? out_pos[c] : c] = e->hbias[l][c];
+    for (int c = 0; c < e->N; ++c) b[p.pos ? p.pos[c] : c] = p.bias[c];
     T(cudaMemcpy(d.bias, b.data(), (size_t)e->N * 4, cudaMemcpyHostToDevice));
   }
-  int32_t max_in_degree = 0;  // counts of the binary first layer must fit 7 bits
-  if (l == 0 && p.constw) {
-    std::vector<int32_t> deg(e->N, 0);
-    for (int32_t c : h->cols) max_in_degree = std::max(max_in_degree, ++deg[c]);
-  }
-  if (rc == cudaSuccess && l == 0 && p.constw && p.max_depth < 128 && max_in_degree < 128) {
+  if (rc == cudaSuccess && l == 0 && p.constw && p.max_depth < 128 && p.max_in_degree < 128) {
     // the float kernel adds w once per active edge: reproduce those sums
     float sums[128];
     float acc = 0.f;
@@ -480,6 +529,15 @@ int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
     return rc == cudaErrorMemoryAllocation ? SDNN_ERR_OOM : SDNN_ERR_CUDA;
   }
   return SDNN_OK;
+}
+
+// Packs layer l with the chosen neuron placement and uploads it.
+int pack_upload_layer(sdnn_engine* e, int l, std::string& err) {
+  PackedLayer p;
+  int32_t maxdeg = 0;
+  int rc = pack_host_layer(e, l, p, maxdeg, err);
+  if (rc) return rc;
+  return upload_layer(e, l, view_of(e, l, p, maxdeg), err);
 }
 
 // Runs fn(l, err) for every layer on a small thread pool; first error wins.
@@ -515,13 +573,32 @@ int for_layers(sdnn_engine* e, Fn fn) {
   return status.load();
 }
 
+// Neuron placement of every layer into e->pos (whole-row layouts): outputs
+// grouped by in-degree, lanes balancing the next layer's bank loads.
+int compute_placement(sdnn_engine* e) {
+  std::vector<std::vector<int32_t>> order(e->L);
+  int rc = for_layers(e, [&](int l, std::string&) {
+    HostLayer tmp;
+    order[l] = degree_order(*host_layer(e, l, tmp), e->N);
+    return SDNN_OK;
+  });
+  if (rc) return rc;
+  e->pos.assign(e->L, {});
+  return for_layers(e, [&](int l, std::string&) {
+    HostLayer tmp;
+    const HostLayer* next = l + 1 < e->L ? host_layer(e, l + 1, tmp) : nullptr;
+    e->pos[l] = place_outputs(order[l], next, next ? &order[l + 1] : nullptr, e->N);
+    return SDNN_OK;
+  });
+}
+
 // Packs every layer.  With whole-row layouts (one chunk) the neurons of each
 // layer are first placed: outputs grouped by in-degree (so the 32 lanes of a
 // group have nearly equal slot lists) and given lanes that balance the bank
 // loads of the next layer, which shortens the bank-scheduled slot lists.
 int finalize_weights(sdnn_engine* e) {
   if (!e->weights_dirty) return SDNN_OK;
-  if (!e->gen.on) {
+  if (!e->gen.on && !e->packed) {
     if ((int)e->hw.size() != e->L) return fail(e, SDNN_ERR_STATE, "weights not loaded");
     for (int l = 0; l < e->L; ++l)
       if (!e->hw[l].present)
@@ -531,26 +608,28 @@ int finalize_weights(sdnn_engine* e) {
   free_weights(e);
   e->dl.assign(e->L, DevLayer{});
   e->pos.clear();
-  const bool place = e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
+  const bool place = !e->packed && e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
   int rc;
-  if (place) {
-    std::vector<std::vector<int32_t>> order(e->L);
-    rc = for_layers(e, [&](int l, std::string&) {
-      HostLayer tmp;
-      order[l] = degree_order(*host_layer(e, l, tmp), e->N);
-      return SDNN_OK;
+  if (e->packed) {
+    // a packed-weight file: its placement and slots as they are, checked first
+    if (e->packed->placed) {
+      e->pos.resize(e->L);
+      for (int l = 0; l < e->L; ++l)
+        e->pos[l].assign(e->packed->layers[l].pos, e->packed->layers[l].pos + e->N);
+    }
+    rc = for_layers(e, [&](int l, std::string& err) {
+      const PackedView& v = e->packed->layers[l];
+      if (!check_view(e, v, err)) {
+        err = "packed weights, layer " + std::to_string(l) + ": " + err;
+        return (int)SDNN_ERR_FORMAT;
+      }
+      return upload_layer(e, l, v, err);
     });
-    if (rc) return rc;
-    e->pos.resize(e->L);
-    rc = for_layers(e, [&](int l, std::string&) {
-      HostLayer tmp;
-      const HostLayer* next = l + 1 < e->L ? host_layer(e, l + 1, tmp) : nullptr;
-      e->pos[l] = place_outputs(order[l], next, next ? &order[l + 1] : nullptr, e->N);
-      return SDNN_OK;
-    });
-    if (rc) return rc;
+  } else if (place) {
+    if ((rc = compute_placement(e))) return rc;
   }
-  rc = for_layers(e, [&](int l, std::string& err) { return pack_upload_layer(e, l, err); });
+  if (!e->packed)
+    rc = for_layers(e, [&](int l, std::string& err) { return pack_upload_layer(e, l, err); });
   if (rc) {
     free_weights(e);
     return rc;
@@ -1189,6 +1268,7 @@ int sdnn_load_weights_tsv(sdnn_engine* e, const char* dir) {
     int rc = read_weight_tsv(p, e->N, e->hw[l], e->err);
     if (rc) return rc;
   }
+  e->packed.reset();
   e->weights_dirty = true;
   return SDNN_OK;
 }
@@ -1203,6 +1283,11 @@ int sdnn_set_layer_coo(sdnn_engine* e, int32_t layer, const int32_t* rows, const
     e->gen.on = false;
     for (auto& h : e->hw) h.present = false;
   }
+  if (e->packed) {
+    // switching from a packed file to explicit weights: the other layers are gone
+    e->packed.reset();
+    for (auto& h : e->hw) h.present = false;
+  }
   if (!coo_to_host_layer(e->N, rows, cols, vals, nnz, e->hw[layer], e->err)) return SDNN_ERR_INVALID;
   e->weights_dirty = true;
   return SDNN_OK;
@@ -1211,6 +1296,8 @@ int sdnn_set_layer_coo(sdnn_engine* e, int32_t layer, const int32_t* rows, const
 int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias) {
   if (!e || !bias) return SDNN_ERR_INVALID;
   if (layer < 0 || layer >= e->L) return fail(e, SDNN_ERR_INVALID, "bad layer");
+  if (e->packed)
+    return fail(e, SDNN_ERR_STATE, "weights come from a packed file (its biases are part of it)");
   if ((int)e->hbias.size() < e->L) e->hbias.resize(e->L);
   e->hbias[layer].assign(bias, bias + e->N);
   e->weights_dirty = true;
@@ -1220,6 +1307,7 @@ int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias) {
 int sdnn_generate_weights(sdnn_engine* e, uint64_t seed, int32_t nnz_per_row, float value) {
   if (!e) return SDNN_ERR_INVALID;
   if (nnz_per_row < 1 || nnz_per_row > e->N) return fail(e, SDNN_ERR_INVALID, "bad nnz_per_row");
+  e->packed.reset();
   e->gen.on = true;
   e->gen.seed = seed;
   e->gen.nnz = nnz_per_row;
@@ -1428,6 +1516,73 @@ int sdnn_get_stats(const sdnn_engine* ce, sdnn_stats* out) {
   return SDNN_OK;
 }
 
+int sdnn_save_packed_weights(sdnn_engine* e, const char* path) {
+  if (!e || !path) return SDNN_ERR_INVALID;
+  const int32_t scale = slot_index_in_bytes(e->Q) ? 4 : 1;
+  PackedWriter w;
+  if (e->packed) {
+    const PackedFile& pf = *e->packed;
+    if (!w.begin(path, pf.N, pf.L, pf.Q, pf.nq, pf.G, pf.placed, pf.scale, e->err))
+      return SDNN_ERR_IO;
+    for (int l = 0; l < pf.L; ++l)
+      if (!w.layer(pf.layers[l], pf.N, pf.G, pf.nq, pf.placed, e->err)) return SDNN_ERR_IO;
+    return w.end(e->err) ? SDNN_OK : SDNN_ERR_IO;
+  }
+  if (!e->gen.on) {
+    if ((int)e->hw.size() != e->L) return fail(e, SDNN_ERR_STATE, "weights not loaded");
+    for (int l = 0; l < e->L; ++l)
+      if (!e->hw[l].present)
+        return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
+  }
+  const bool place = e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
+  int rc;
+  if (place) {
+    if ((rc = compute_placement(e))) return rc;
+  } else {
+    e->pos.clear();
+  }
+  if (!w.begin(path, e->N, e->L, e->Q, e->nq, e->G, place, scale, e->err)) return SDNN_ERR_IO;
+  // pack a batch of layers in parallel, write it in order, next batch
+  const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  for (int b0 = 0; b0 < e->L; b0 += nt) {
+    const int b1 = std::min(e->L, b0 + nt);
+    std::vector<PackedLayer> packs(b1 - b0);
+    std::vector<int32_t> maxdeg(b1 - b0, 0);
+    std::vector<std::string> errs(b1 - b0);
+    std::vector<int> rcs(b1 - b0, SDNN_OK);
+    std::vector<std::thread> pool;
+    for (int l = b0; l < b1; ++l)
+      pool.emplace_back([&, l] { rcs[l - b0] = pack_host_layer(e, l, packs[l - b0], maxdeg[l - b0], errs[l - b0]); });
+    for (auto& t : pool) t.join();
+    for (int l = b0; l < b1; ++l) {
+      if (rcs[l - b0]) return fail(e, rcs[l - b0], errs[l - b0]);
+      if (!w.layer(view_of(e, l, packs[l - b0], maxdeg[l - b0]), e->N, e->G, e->nq, place, e->err))
+        return SDNN_ERR_IO;
+    }
+  }
+  return w.end(e->err) ? SDNN_OK : SDNN_ERR_IO;
+}
+
+int sdnn_load_packed_weights(sdnn_engine* e, const char* path) {
+  if (!e || !path) return SDNN_ERR_INVALID;
+  std::string err;
+  std::shared_ptr<PackedFile> pf = open_packed_file(path, err);
+  if (!pf) return fail(e, err.rfind("cannot", 0) == 0 ? SDNN_ERR_IO : SDNN_ERR_FORMAT, err);
+  const int32_t scale = slot_index_in_bytes(e->Q) ? 4 : 1;
+  if (pf->N != e->N || pf->L != e->L || pf->Q != e->Q || pf->nq != e->nq || pf->G != e->G ||
+      pf->scale != scale)
+    return fail(e, SDNN_ERR_FORMAT,
+                std::string(path) + ": packed for N=" + std::to_string(pf->N) + ", L=" +
+                    std::to_string(pf->L) + ", chunk " + std::to_string(pf->Q) +
+                    ", not this engine's layout");
+  e->packed = pf;
+  e->gen.on = false;
+  for (auto& h : e->hw) h = HostLayer{};
+  e->hbias.clear();
+  e->weights_dirty = true;
+  return SDNN_OK;
+}
+
 int sdnn_set_mode(sdnn_engine* e, int32_t mode, int32_t threshold) {
   if (!e || mode < SDNN_MODE_BF || mode > SDNN_MODE_SNICIT || threshold < 0) return SDNN_ERR_INVALID;
   e->cfg.mode = mode;
@@ -1540,6 +1695,7 @@ cudaStream_t engine_stream(const sdnn_engine* e) { return e->stream; }
 
 // ---- hooks for the serving loop (serve.cpp)
 void engine_copy_weights(sdnn_engine* dst, const sdnn_engine* src) {
+  dst->packed = src->packed;
   dst->gen = src->gen;
   dst->hw = src->hw;
   dst->hbias = src->hbias;

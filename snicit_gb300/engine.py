@@ -166,6 +166,14 @@ class Engine:
         self._ck(load().sdnn_get_layer_rows(self._h, _ptr(out), self.L))
         return out
 
+    def save_packed(self, path):
+        """Writes the packed weights (host packing; no GPU needed)."""
+        self._ck(load().sdnn_save_packed_weights(self._h, str(path).encode()))
+
+    def load_packed(self, path):
+        """Takes the weights from a packed-weight file (mmap)."""
+        self._ck(load().sdnn_load_packed_weights(self._h, str(path).encode()))
+
     def set_mode(self, mode, threshold=None):
         """Switches mode (and threshold) keeping the packed weights."""
         m = _lib.MODES[mode] if isinstance(mode, str) else int(mode)
@@ -249,3 +257,26 @@ def write_inputs_tsv(path, Y0):
 def write_categories_tsv(path, ids):
     ids = np.ascontiguousarray(ids, dtype=np.int32)
     check(load().sdnn_write_categories_tsv(str(path).encode(), _ptr(ids), len(ids)))
+
+
+def write_inputs_bin(path, Y0, bits=False):
+    """Binary input file: FP32 rows, or one bit per entry (0/1 inputs)."""
+    Y0 = np.ascontiguousarray(Y0, dtype=np.float32)
+    check(load().sdnn_write_inputs_bin(str(path).encode(), _ptr(Y0), Y0.shape[0], Y0.shape[1],
+                                       1 if bits else 0))
+
+
+def inputs_bin_info(path):
+    n, r, enc = ctypes.c_int32(0), ctypes.c_int64(0), ctypes.c_int32(0)
+    check(load().sdnn_inputs_bin_info(str(path).encode(), ctypes.byref(n), ctypes.byref(r),
+                                      ctypes.byref(enc)))
+    return n.value, r.value, enc.value
+
+
+def read_inputs_bin(path, num_neurons, row_offset=0, rows=None):
+    if rows is None:
+        rows = inputs_bin_info(path)[1] - row_offset
+    out = np.zeros((rows, num_neurons), dtype=np.float32)
+    check(load().sdnn_read_inputs_bin(str(path).encode(), int(num_neurons), int(row_offset),
+                                      int(rows), _ptr(out)))
+    return out

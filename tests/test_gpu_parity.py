@@ -432,3 +432,21 @@ def test_set_mode_and_device_autotune():
             eng.infer_device(d.data_ptr(), B, f.data_ptr())
             torch.cuda.synchronize()
             assert np.array_equal(f.cpu().numpy(), alive), mode
+
+
+@pytest.mark.parametrize("N,L,B", [(1024, 40, 500), (65536, 3, 64)])
+def test_packed_weight_file_gives_the_same_inference(tmp_path, N, L, B):
+    seed = 61
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    path = tmp_path / "w.sdnnw"
+    with sg.Engine(N, L, mode="SNICIT", threshold=min(20, L - 1), batch=B) as eng:
+        eng.generate_weights(seed)
+        eng.save_packed(path)
+        f1, ids1 = eng.infer(Y0)
+        y1 = eng.activations(B)
+    with sg.Engine(N, L, mode="SNICIT", threshold=min(20, L - 1), batch=B) as eng:
+        eng.load_packed(path)
+        f2, ids2 = eng.infer(Y0)
+        y2 = eng.activations(B)
+    assert np.array_equal(ids1, ids2)
+    assert np.array_equal(y1.view(np.uint32), y2.view(np.uint32))
