@@ -100,7 +100,7 @@ int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
   const int tile_stage =
       (cfg0.mode == SDNN_MODE_SNICIT && cfg0.threshold > 0 && cfg0.threshold < cfg0.num_layers) ? 0 : -1;
   for (int tile : tiles) {
-    for (int threads : {256, 512}) {
+    for (int threads : {256, 512, 1024}) {
       Trial t{tile, threads, cfg0.threshold, cfg0.num_centroids, cfg0.merge_start, 0.f, 0, 0};
       t.status = sdnn::engine_set_tile(e, tile, threads);
       if (t.status == SDNN_OK) t.status = time_setting(e, smp, tile_stage, t.ms, t.survivors);

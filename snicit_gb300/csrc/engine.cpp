@@ -275,7 +275,7 @@ int choose_kernel(sdnn_engine* e) {
   const int N = e->N;
   const int req_T = e->cfg.tile_rows;
   int threads = e->cfg.threads > 0 ? e->cfg.threads : 512;
-  if (threads != 256 && threads != 512) threads = 512;
+  if (threads != 256 && threads != 512 && threads != 1024) threads = 512;
   std::vector<LayerKernelKey> cands;
   if (e->nq == 1) {
     int rsw = e->Q == 1024 ? 1056 : e->Q == 4096 ? 4128 : e->Q == 16384 ? 16416 : 0;
