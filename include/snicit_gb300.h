@@ -188,6 +188,13 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows,
  * synchronize; SNICIT waits once, after the threshold clustering, to read how
  * many residue rows and centroids it produced (which picks the kernels for the
  * remaining layers). */
+/* The same with one-bit input rows (entry j of a row in bit j % 64 of word
+ * j / 64, ceil(N / 64) words per row -- the layout of the bit-encoded input
+ * files): 32x fewer bytes over the host link for 0/1 inputs such as the SDGC
+ * images; the rows are expanded on the device.  N must be a multiple of 4. */
+int sdnn_infer_host_bits(sdnn_engine* e, const uint64_t* bits, int64_t rows, int32_t* flags,
+                         int32_t* ids, int64_t* count);
+
 int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
                       int32_t* d_flags, void* stream);
 

@@ -92,6 +92,7 @@ SIGNATURES = [
     ("sdnn_finalize_weights", ctypes.c_int, [P]),
     ("sdnn_infer_host", ctypes.c_int, [P, P, I64, P, P, P]),
     ("sdnn_infer_device", ctypes.c_int, [P, P, I64, P, P]),
+    ("sdnn_infer_host_bits", ctypes.c_int, [P, P, I64, P, P, P]),
     ("sdnn_infer_batches_host", ctypes.c_int, [P, P, P, I32, P]),
     ("sdnn_infer_batches_device", ctypes.c_int, [P, P, P, I32, P, P]),
     ("sdnn_read_inputs_tsv", ctypes.c_int, [ctypes.c_char_p, I32, I64, I64, P]),

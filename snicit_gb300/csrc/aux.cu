@@ -516,3 +516,29 @@ bool launch_head(const float* y, const int32_t* state, const int32_t* cslot, con
 }
 
 }  // namespace sdnn
+
+namespace sdnn {
+
+// One-bit input rows (entry j in bit j % 64 of word j / 64, ceil(N / 64) words
+// per row) to FP32 0/1 rows; one thread writes four consecutive entries.
+__global__ void expand_bits_kernel(const unsigned long long* __restrict__ bits, int64_t rows,
+                                   int32_t N, float4* out) {
+  const int32_t W = (N + 63) / 64, n4 = N / 4;
+  const int64_t total = rows * n4;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / n4;
+    const int32_t j = (int32_t)(i % n4) * 4;
+    const unsigned long long w = __ldg(bits + r * W + (j >> 6));
+    const uint32_t b = (uint32_t)(w >> (j & 63)) & 15u;
+    out[i] = make_float4(b & 1u ? 1.f : 0.f, b & 2u ? 1.f : 0.f, b & 4u ? 1.f : 0.f,
+                         b & 8u ? 1.f : 0.f);
+  }
+}
+
+void launch_expand_bits(const uint64_t* bits, int64_t rows, int32_t N, float* out, cudaStream_t s) {
+  expand_bits_kernel<<<4096, 256, 0, s>>>(reinterpret_cast<const unsigned long long*>(bits), rows,
+                                          N, reinterpret_cast<float4*>(out));
+}
+
+}  // namespace sdnn

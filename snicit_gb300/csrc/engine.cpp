@@ -127,6 +127,8 @@ struct sdnn_engine {
   int32_t* d_rows = nullptr;      // row count of the current inference
   int32_t* d_fallback = nullptr;  // layer-0 rows of non-binary tiles
   int32_t* d_fbcount = nullptr;
+  uint64_t* d_inbits = nullptr;    // one-bit host inputs, staged before expansion
+  int64_t inbits_cap = 0;
   float* d_gscratch = nullptr;     // grid chain: [2][8][nq][Q + 32] centroid rows
   unsigned int* d_gbar = nullptr;  // grid chain barrier counter
   uint32_t* d_bits = nullptr;      // chunked binary first layer: bit words per 32-row tile
@@ -231,6 +233,8 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_tile_state);
   dfree(e->d_gscratch);
   dfree(e->d_gbar);
+  dfree(e->d_inbits);
+  e->inbits_cap = 0;
   dfree(e->d_rows);
   dfree(e->d_alias);
   dfree(e->d_mtable);
@@ -1349,18 +1353,32 @@ int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows, int32_t* 
   return rc;
 }
 
-int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows, int32_t* flags, int32_t* ids,
-                    int64_t* count) {
-  if (!e || !Y0 || rows <= 0) return SDNN_ERR_INVALID;
+// Host inference over batches of cfg.batch rows; inputs as FP32 rows, or as
+// one-bit rows (bits != nullptr) expanded on the device.
+int infer_host(sdnn_engine* e, const float* Y0, const uint64_t* bits, int64_t rows, int32_t* flags,
+               int32_t* ids, int64_t* count) {
   int rc = prepare(e, std::min<int64_t>(rows, e->cfg.batch));
   if (rc) return rc;
   const int64_t N = e->N;
+  const int64_t W = (N + 63) / 64;
+  if (bits && e->inbits_cap < e->cap) {
+    dfree(e->d_inbits);
+    CK(cudaMalloc((void**)&e->d_inbits, (size_t)e->cap * W * 8));
+    e->inbits_cap = e->cap;
+  }
   int64_t total = 0;
   sdnn_stats acc{};
   for (int64_t off = 0; off < rows; off += e->cfg.batch) {
     const int64_t n = std::min<int64_t>(e->cfg.batch, rows - off);
-    CK(cudaMemcpyAsync(e->d_in, Y0 + off * N, (size_t)(n * N) * 4, cudaMemcpyHostToDevice,
-                       e->stream));
+    if (bits) {
+      CK(cudaMemcpyAsync(e->d_inbits, bits + off * W, (size_t)(n * W) * 8, cudaMemcpyHostToDevice,
+                         e->stream));
+      launch_expand_bits(e->d_inbits, n, e->N, e->d_in, e->stream);
+      CK(cudaGetLastError());
+    } else {
+      CK(cudaMemcpyAsync(e->d_in, Y0 + off * N, (size_t)(n * N) * 4, cudaMemcpyHostToDevice,
+                         e->stream));
+    }
     rc = run(e, n, e->d_in, e->d_flags);
     if (rc) return rc;
     if (ids || count) {
@@ -1399,6 +1417,19 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows, int32_t* flag
   e->stats = acc;
   if (count) *count = total;
   return SDNN_OK;
+}
+
+int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows, int32_t* flags, int32_t* ids,
+                    int64_t* count) {
+  if (!e || !Y0 || rows <= 0) return SDNN_ERR_INVALID;
+  return infer_host(e, Y0, nullptr, rows, flags, ids, count);
+}
+
+int sdnn_infer_host_bits(sdnn_engine* e, const uint64_t* bits, int64_t rows, int32_t* flags,
+                         int32_t* ids, int64_t* count) {
+  if (!e || !bits || rows <= 0) return SDNN_ERR_INVALID;
+  if (e->N % 4) return fail(e, SDNN_ERR_UNSUPPORTED, "one-bit inputs need N % 4 == 0");
+  return infer_host(e, nullptr, bits, rows, flags, ids, count);
 }
 
 int sdnn_infer_batches_host(sdnn_engine* e, const float* const* inputs, const int64_t* rows,

@@ -117,6 +117,19 @@ class Engine:
                                         ctypes.byref(count)))
         return flags, (ids[: count.value].copy() if ids is not None else None)
 
+    def infer_bits(self, bits, want_flags=True, want_ids=True):
+        """Host inference on one-bit rows (uint64 array rows x ceil(N / 64),
+        see pack_bits); returns (flags or None, sorted survivor ids or None)."""
+        bits = np.ascontiguousarray(bits, dtype=np.uint64)
+        assert bits.ndim == 2 and bits.shape[1] == (self.N + 63) // 64
+        rows = bits.shape[0]
+        flags = np.zeros(rows, dtype=np.int32) if want_flags else None
+        ids = np.zeros(rows, dtype=np.int32) if want_ids else None
+        count = ctypes.c_int64(0)
+        self._ck(load().sdnn_infer_host_bits(self._h, _ptr(bits), rows, _ptr(flags), _ptr(ids),
+                                             ctypes.byref(count)))
+        return flags, (ids[: count.value].copy() if ids is not None else None)
+
     def infer_device(self, y0_ptr, rows, flags_ptr, stream_ptr=None):
         """Device inference on raw device pointers (e.g. torch tensor data_ptr())."""
         self._ck(load().sdnn_infer_device(self._h, ctypes.c_void_p(int(y0_ptr)), int(rows),
@@ -280,3 +293,14 @@ def read_inputs_bin(path, num_neurons, row_offset=0, rows=None):
     check(load().sdnn_read_inputs_bin(str(path).encode(), int(num_neurons), int(row_offset),
                                       int(rows), _ptr(out)))
     return out
+
+
+def pack_bits(Y0):
+    """0/1 rows to the one-bit layout (uint64 words, entry j in bit j % 64 of word j / 64)."""
+    Y0 = np.asarray(Y0)
+    rows, N = Y0.shape
+    W = (N + 63) // 64
+    padded = np.zeros((rows, W * 64), dtype=np.uint8)
+    padded[:, :N] = Y0 != 0
+    return np.packbits(padded.reshape(rows, W, 64)[:, :, ::-1], axis=2).reshape(rows, W, 8)[:, :, ::-1] \
+        .copy().view(np.uint64).reshape(rows, W)

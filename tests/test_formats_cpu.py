@@ -91,3 +91,12 @@ def test_binary_inputs_errors(tmp_path):
     (tmp_path / "z.bin").write_bytes(b"not an input file at all, really")
     with pytest.raises(SdnnError):
         sg.inputs_bin_info(tmp_path / "z.bin")
+
+
+def test_pack_bits_matches_the_file_encoding(tmp_path):
+    N = 1000
+    Y = sg.generate_inputs(N, 9, 0, 11)
+    path = tmp_path / "in.bin"
+    sg.write_inputs_bin(path, Y, bits=True)
+    words = np.frombuffer(path.read_bytes()[32:], dtype=np.uint64).reshape(11, -1)
+    assert np.array_equal(sg.pack_bits(Y), words)

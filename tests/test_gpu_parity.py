@@ -450,3 +450,14 @@ def test_packed_weight_file_gives_the_same_inference(tmp_path, N, L, B):
         y2 = eng.activations(B)
     assert np.array_equal(ids1, ids2)
     assert np.array_equal(y1.view(np.uint32), y2.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ["SNIG", "SNICIT"])
+def test_one_bit_host_inputs_match_float_inputs(mode):
+    N, L, B, seed = 1024, 30, 900, 71
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    with sg.Engine(N, L, mode=mode, threshold=12, batch=400, bias=-0.3) as eng:
+        eng.generate_weights(seed)
+        f1, ids1 = eng.infer(Y0)
+        f2, ids2 = eng.infer_bits(sg.pack_bits(Y0))
+    assert np.array_equal(f1, f2) and np.array_equal(ids1, ids2)
