@@ -153,6 +153,78 @@ __device__ __forceinline__ void accumulate_group(float (&acc)[T], const LayerDev
   }
 }
 
+// Input chunks: the KG groups of a warp (gbeg + warp + kk * nwarps) over
+// chunk q.  Their lists are short (about 8 slots per lane and chunk), so
+// fetching them group by group costs a memory round trip per group; here the
+// KG offsets come in one load (lane kk holds group kk's), and the first
+// CHUNK_NB blocks of group kk + 1 are loaded while group kk is applied.  The
+// FMA order of every group is unchanged (blocks, then slots, in order).
+constexpr int CHUNK_NB = 4;
+template <int T, int RSW, bool CONSTW, int KG>
+__device__ __forceinline__ void accumulate_chunk(float (&acc)[KG][T], const LayerDev& wl, int nq,
+                                                 const float* __restrict__ ys, int RS, int gbeg,
+                                                 int gend, int warp, int nwarps, int q, int lane) {
+  int32_t my_b0 = 0, my_b1 = 0;
+  if (lane < KG) {
+    const int g = gbeg + warp + lane * nwarps;
+    if (g < gend) {
+      my_b0 = __ldg(wl.grp_blk + g * nq + q);
+      my_b1 = __ldg(wl.grp_blk + g * nq + q + 1);
+    }
+  }
+  const float wc = wl.wconst;
+  uint2 iv[2][CHUNK_NB];
+  float4 vv[2][CONSTW ? 1 : CHUNK_NB];
+  auto fetch = [&](int kk, uint2 (&i)[CHUNK_NB], float4 (&v)[CONSTW ? 1 : CHUNK_NB]) {
+    const int32_t b0 = __shfl_sync(0xffffffffu, my_b0, kk);
+    const int nb = __shfl_sync(0xffffffffu, my_b1, kk) - b0;
+    const uint2* ip = wl.idx + (size_t)b0 * 32 + lane;
+#pragma unroll
+    for (int k = 0; k < CHUNK_NB; ++k) {
+      if (k < nb) {
+        i[k] = __ldg(ip + (size_t)k * 32);
+        if constexpr (!CONSTW) v[k] = __ldg(wl.val + (size_t)(b0 + k) * 32 + lane);
+      }
+    }
+  };
+  fetch(0, iv[0], vv[0]);
+#pragma unroll
+  for (int kk = 0; kk < KG; ++kk) {
+    const int cur = kk & 1;
+    if (kk + 1 < KG) fetch(kk + 1, iv[cur ^ 1], vv[cur ^ 1]);
+    const int32_t b0 = __shfl_sync(0xffffffffu, my_b0, kk);
+    const int nb = __shfl_sync(0xffffffffu, my_b1, kk) - b0;
+    // the first CHUNK_NB blocks (prefetched), one at a time in order
+#pragma unroll
+    for (int k = 0; k < CHUNK_NB; ++k) {
+      if (k < nb) {
+        uint2 one[1] = {iv[cur][k]};
+        float4 onev[1];
+        if constexpr (!CONSTW) onev[0] = vv[cur][k];
+        apply_blocks<T, RSW, CONSTW, 1>(acc[kk], one, onev, wc, ys, RS);
+      }
+    }
+    // the rest of a long list, in exact-size batches
+    if (nb > CHUNK_NB) {
+      const uint2* ip = wl.idx + (size_t)b0 * 32 + lane;
+      const float4* vp = CONSTW ? nullptr : wl.val + (size_t)b0 * 32 + lane;
+      int b = CHUNK_NB;
+      for (; b + 4 <= nb; b += 4) {
+        uint2 i4[4];
+        float4 v4[CONSTW ? 1 : 4];
+        load_blocks<CONSTW, 4>(i4, v4, ip, vp, b);
+        apply_blocks<T, RSW, CONSTW, 4>(acc[kk], i4, v4, wc, ys, RS);
+      }
+      for (; b < nb; ++b) {
+        uint2 i1[1];
+        float4 v1[1];
+        load_blocks<CONSTW, 1>(i1, v1, ip, vp, b);
+        apply_blocks<T, RSW, CONSTW, 1>(acc[kk], i1, v1, wc, ys, RS);
+      }
+    }
+  }
+}
+
 // Epilogue of one group for the rows of the tile; returns the row mask of
 // rows flagged by this warp (alive for PLAIN, non-empty for RESIDUE).
 template <int T>
@@ -342,11 +414,8 @@ __global__ void __launch_bounds__(KG == 1 ? 1024 : 512) layer_kernel(const Layer
         if (s_fail) return;
         mbar_try_wait(&bar[0], phase);
         phase ^= 1u;
-#pragma unroll
-        for (int kk = 0; kk < KG; ++kk) {
-          const int g = gbeg + warp + kk * nwarps;
-          if (g < gend) accumulate_group<T, RSW, CONSTW>(acc[kk], a.w, a.nq, ys, RS, g, q, lane);
-        }
+        accumulate_chunk<T, RSW, CONSTW, KG>(acc, a.w, a.nq, ys, RS, gbeg, gend, warp, nwarps, q,
+                                             lane);
       }
       uint32_t m = 0;
 #pragma unroll
