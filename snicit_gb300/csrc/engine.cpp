@@ -294,8 +294,10 @@ int choose_kernel(sdnn_engine* e) {
     if (rsw == 16416)
       for (int T : {8, 4, 2, 1}) cands.push_back({T, 0, 1, true});
   } else {
+    // 16 groups per warp at 512 threads, 8 at 1024 (the same groups per CTA)
+    const int kg = threads == 1024 ? 8 : 16;
     if (e->Q == 16384)
-      for (int T : {3, 2, 1}) cands.push_back({T, 16416, 16, true});
+      for (int T : {3, 2, 1}) cands.push_back({T, 16416, kg, true});
     cands.push_back({1, 0, 16, true});
   }
   for (const auto& k : cands) {

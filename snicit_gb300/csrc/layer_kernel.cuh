@@ -324,9 +324,9 @@ __device__ __forceinline__ void publish_rows(const LayerArgs& a, uint32_t m, int
 }
 
 template <int T, int RSW, int KG, bool CONSTW>
-// (whole-row instances may run 1024 threads; chunked ones keep 512 so their
-// KG x T accumulators stay in registers)
-__global__ void __launch_bounds__(KG == 1 ? 1024 : 512) layer_kernel(const LayerArgs a) {
+// (instances with up to 8 groups per warp may run 1024 threads; 16 groups per
+// warp keep 512 so their KG x T accumulators stay in registers)
+__global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const LayerArgs a) {
   extern __shared__ __align__(128) float ys[];
   __shared__ __align__(8) uint64_t bar[1];
   __shared__ int32_t s_rows[1][T];

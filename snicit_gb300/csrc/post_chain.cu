@@ -30,7 +30,7 @@ namespace sdnn {
 constexpr int kChainCluster = 8;
 
 template <int RSW, int KC>
-__global__ void __launch_bounds__(512, 1) chain_kernel(const ChainArgs a) {
+__global__ void __launch_bounds__(1024, 1) chain_kernel(const ChainArgs a) {
   extern __shared__ __align__(128) float rows[];  // [2][KC][RSW]
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -445,6 +445,12 @@ ChainPlan chain_plan(const ChainArgs& a, int kc_needed) {
   p.cluster = kChainCluster;
   p.threads = 512;
   p.smem = (size_t)2 * kc * rsw * sizeof(float);
+  // wide rows (many groups per CTA): a cluster of 16 and 1024 threads, one
+  // group per warp at N = 16384
+  if (a.G / kChainCluster > 32 && cluster16_ok(chain_fn(rsw, kc), 1024, p.smem)) {
+    p.cluster = 16;
+    p.threads = 1024;
+  }
   if (!a.stream) return p;
   const int threads2 = (kChain2ComputeWarps + 1) * 32;
   // streamed weights: cluster 8 with two weight buffers, else 16 with two or one
