@@ -223,7 +223,7 @@ def run_ours(args):
     weights = load_weights(eng, args, N, L)
     pack_s = time.perf_counter() - t0
     if not args.no_autotune and not args.tile:
-        rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
+        rec = os.path.join(args.record_dir, f"autotune_{args.workload}.jsonl")
         os.makedirs(os.path.dirname(rec), exist_ok=True)
         if os.path.exists(rec):
             os.remove(rec)
@@ -425,7 +425,7 @@ def run_uneven(args):
     eng.finalize()
     pack_s = time.perf_counter() - t0
     if not args.no_autotune and not args.tile:
-        rec = os.path.join(ROOT, "gpurun_out", f"autotune_{args.workload}.jsonl")
+        rec = os.path.join(args.record_dir, f"autotune_{args.workload}.jsonl")
         os.makedirs(os.path.dirname(rec), exist_ok=True)
         if os.path.exists(rec):
             os.remove(rec)
@@ -592,6 +592,8 @@ def main():
     ap.add_argument("--merge-start", type=int, default=0,
                     help="first layer after which identical rows merge (0 = default/autotuned)")
     ap.add_argument("--merge-every", type=int, default=0)
+    ap.add_argument("--record-dir", default=os.path.join(ROOT, "records"),
+                    help="where the autotuner's JSON-lines record of its sweep goes")
     ap.add_argument("--weights-cache", default=None,
                     help="directory of packed-weight files (written on the first run)")
     ap.add_argument("--no-cpu", action="store_true")
