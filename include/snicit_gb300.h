@@ -233,6 +233,13 @@ int sdnn_get_stats(const sdnn_engine* e, sdnn_stats* out);
 int sdnn_save_packed_weights(sdnn_engine* e, const char* path);
 int sdnn_load_packed_weights(sdnn_engine* e, const char* path);
 
+/* Self-test of failure detection (no reference counterpart; the reference
+ * exits on errors, src/SDGC/gpu_lib/gpu_runtime.h:2-17): runs one device wait
+ * that nothing completes, bounded by limit_us (<= 10 s), through the same
+ * helper every kernel wait uses.  Returns SDNN_ERR_TIMEOUT when the wait ran
+ * out as it must; the engine stays usable afterwards. */
+int sdnn_selftest_wait_timeout(sdnn_engine* e, int64_t limit_us);
+
 /* Switches the mode (and threshold) of an engine without repacking its
  * weights, e.g. to time the plain path and SNICIT on one resident copy of W.
  * (The reference picks the engine class once, main/SDGC.cu:104-110.) */

@@ -102,6 +102,7 @@ SIGNATURES = [
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_autotune_device", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_set_mode", ctypes.c_int, [P, I32, I32]),
+    ("sdnn_selftest_wait_timeout", ctypes.c_int, [P, I64]),
     ("sdnn_save_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_load_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_layer_noalloc", ctypes.c_int, [P, I32, P, P, I64, P, P]),

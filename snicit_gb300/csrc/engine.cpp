@@ -1616,6 +1616,14 @@ int sdnn_load_packed_weights(sdnn_engine* e, const char* path) {
   return SDNN_OK;
 }
 
+int sdnn_selftest_wait_timeout(sdnn_engine* e, int64_t limit_us) {
+  if (!e || limit_us <= 0 || limit_us > 10000000) return SDNN_ERR_INVALID;
+  int rc = prepare(e, 1);
+  if (rc) return rc;
+  CK(launch_wait_selftest(e->d_err, (uint64_t)limit_us * 1000ull, e->stream));
+  return check_device_error(e);  // SDNN_ERR_TIMEOUT expected; resets the error word
+}
+
 int sdnn_set_mode(sdnn_engine* e, int32_t mode, int32_t threshold) {
   if (!e || mode < SDNN_MODE_BF || mode > SDNN_MODE_SNICIT || threshold < 0) return SDNN_ERR_INVALID;
   e->cfg.mode = mode;

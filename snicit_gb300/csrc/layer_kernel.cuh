@@ -55,12 +55,14 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for an mbarrier phase for at most ~2 s; on timeout records DEV_TIMEOUT.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int32_t* err) {
+// Waits for an mbarrier phase for at most limit_ns (default 2 s); on timeout
+// records DEV_TIMEOUT in the error word and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int32_t* err,
+                                                  uint64_t limit_ns = 2000000000ull) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > 2000000000ull) {
+    if (global_ns() - t0 > limit_ns) {
       atomicExch(err, DEV_TIMEOUT);
       return false;
     }

@@ -220,6 +220,9 @@ bool launch_head(const float* y, const int32_t* state, const int32_t* cslot, con
                  const float* Hp, const float* hb, int32_t H, int32_t N, int32_t rows,
                  float* logits, int32_t* argmax, cudaStream_t s);
 
+// A bounded wait that nothing completes (selftest.cu): sets DEV_TIMEOUT.
+cudaError_t launch_wait_selftest(int32_t* err, uint64_t limit_ns, cudaStream_t s);
+
 // One-bit input rows (ceil(N / 64) words per row, N % 4 == 0) to FP32 rows.
 void launch_expand_bits(const uint64_t* bits, int64_t rows, int32_t N, float* out, cudaStream_t s);
 

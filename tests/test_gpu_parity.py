@@ -461,3 +461,18 @@ def test_one_bit_host_inputs_match_float_inputs(mode):
         f1, ids1 = eng.infer(Y0)
         f2, ids2 = eng.infer_bits(sg.pack_bits(Y0))
     assert np.array_equal(f1, f2) and np.array_equal(ids1, ids2)
+
+
+def test_bounded_wait_times_out_and_engine_stays_usable():
+    """Failure detection without a fault: a device wait that nothing completes
+    runs out (0.2 s), the engine reports the timeout, then infers normally."""
+    N, L, B, seed = 1024, 8, 64, 5
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    with sg.Engine(N, L, mode="SNIG", batch=B, bias=-0.3) as eng:
+        eng.generate_weights(seed)
+        rc = sg.load().sdnn_selftest_wait_timeout(eng._h, 200000)
+        assert rc == 7, rc  # SDNN_ERR_TIMEOUT
+        assert b"timed out" in sg.load().sdnn_last_error(eng._h)
+        flags, ids = eng.infer(Y0)
+    _, alive, _ = orc.infer(_layers(N, L, seed), N, -0.3, Y0, precision=64, want_y=False)
+    assert np.array_equal(flags, alive)
