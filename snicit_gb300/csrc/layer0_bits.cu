@@ -32,10 +32,136 @@ __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32
   l = u ^ c;
 }
 
+// ---- epilogue: per-row counts out of the bit-sliced counters ----------------
+//
+// Rows of a tile are bits of the counter planes P[0..6] (P[i] bit t = bit i of
+// row t's count).  With a scalar bias the output of a row depends on its count
+// only, through a 128-entry table, and the rows that survive are those whose
+// count lies in an interval, so:
+//  * the survivor mask of all 32 rows comes from bitwise comparisons of the
+//    planes with the interval's end (no per-row vote);
+//  * the counts come out four 8 x 8 bit-matrix transposes (plane bytes ->
+//    row bytes; the three-step transpose of Hacker's Delight, section 7-3).
+
+// Rows whose count is >= k0 (k0 in 0..128).
+__device__ __forceinline__ uint32_t count_ge(const uint32_t (&P)[7], uint32_t k0) {
+  if (k0 >= 128u) return 0u;
+  uint32_t gt = 0u, eq = 0xffffffffu;
+#pragma unroll
+  for (int i = 6; i >= 0; --i) {
+    if ((k0 >> i) & 1u) eq &= P[i];
+    else gt |= eq & P[i];
+  }
+  return gt | eq;
+}
+
+__device__ __forceinline__ unsigned long long transpose8x8(unsigned long long x) {
+  unsigned long long t;
+  t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
+  x = x ^ t ^ (t << 7);
+  t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull;
+  x = x ^ t ^ (t << 14);
+  t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull;
+  x = x ^ t ^ (t << 28);
+  return x;
+}
+
+// Byte b of each of the planes P[0..6] (plane 7 = 0) as one 64-bit word.
+__device__ __forceinline__ unsigned long long plane_bytes(const uint32_t (&P)[7], int b) {
+  const uint32_t sel = (uint32_t)b | ((uint32_t)(b + 4) << 4);
+  const uint32_t p01 = __byte_perm(P[0], P[1], sel), p23 = __byte_perm(P[2], P[3], sel);
+  const uint32_t p45 = __byte_perm(P[4], P[5], sel), p67 = __byte_perm(P[6], 0u, sel);
+  const uint32_t lo = __byte_perm(p01, p23, 0x5410), hi = __byte_perm(p45, p67, 0x5410);
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+// Survivor interval of the counts for a scalar bias: kind 1 = [k0, 127],
+// kind 2 = [0, k1]; kind 0 = per-neuron bias or no interval (generic path).
+struct CountInterval {
+  int kind;
+  uint32_t lo, hi;
+};
+
+__device__ CountInterval count_interval(const float* s_sum, float bias, bool per_neuron) {
+  __shared__ uint32_t s_alive[4];
+  __shared__ CountInterval s_iv;
+  const int tid = threadIdx.x;
+  if (tid < 128) {
+    const uint32_t m = __ballot_sync(0xffffffffu, s_sum[tid] + bias > 0.f);
+    if ((tid & 31) == 0) s_alive[tid >> 5] = m;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    CountInterval iv{0, 0u, 0u};
+    if (!per_neuron) {
+      // alive counts as a 128-bit set; suffix [k0, 127] or prefix [0, k1]?
+      int first = -1, last = -1;
+      for (int k = 0; k < 128; ++k)
+        if ((s_alive[k >> 5] >> (k & 31)) & 1u) {
+          if (first < 0) first = k;
+          last = k;
+        }
+      int n = 0;
+      for (int w = 0; w < 4; ++w) n += __popc(s_alive[w]);
+      if (first < 0) {
+        iv = {1, 128u, 0u};  // nothing survives: k >= 128 never holds
+      } else if (n == last - first + 1 && last == 127) {
+        iv = {1, (uint32_t)first, 0u};
+      } else if (n == last - first + 1 && first == 0) {
+        iv = {2, 0u, (uint32_t)last};
+      }
+    }
+    s_iv = iv;
+  }
+  __syncthreads();
+  return s_iv;
+}
+
+// Outputs of one group for the rows of a tile from its counters.
+__device__ __forceinline__ uint32_t bits_epilogue(const uint32_t (&P)[7], const Layer0Args& a,
+                                                  const float* s_sum, const float* s_val,
+                                                  const CountInterval& iv, const int32_t* s_rows,
+                                                  int nrows, int c_out, int lane) {
+  const int N = a.N;
+  uint32_t m = 0;
+  if (iv.kind != 0) {
+    const uint32_t rows_mask = nrows >= 32 ? 0xffffffffu : ((1u << nrows) - 1u);
+    uint32_t alive = iv.kind == 1 ? count_ge(P, iv.lo) : ~count_ge(P, iv.hi + 1u);
+    m = __reduce_or_sync(0xffffffffu, alive & rows_mask);
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      if (8 * b >= nrows) break;
+      const unsigned long long x = transpose8x8(plane_bytes(P, b));
+#pragma unroll
+      for (int tp = 0; tp < 8; ++tp) {
+        const int t = 8 * b + tp;
+        if (t < nrows) {
+          const uint32_t k = (uint32_t)(x >> (8 * tp)) & 0x7fu;
+          a.y_out[(size_t)s_rows[t] * N + c_out] = s_val[k];
+        }
+      }
+    }
+    return m;
+  }
+  const float bc = a.bias_vec ? __ldg(a.bias_vec + c_out) : a.bias;
+  for (int t = 0; t < nrows; ++t) {
+    uint32_t k = 0;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) k |= ((P[i] >> t) & 1u) << i;
+    const float v = s_sum[k] + bc;
+    a.y_out[(size_t)s_rows[t] * N + c_out] = clampf(v, a.clampv);
+    if (__any_sync(0xffffffffu, v > 0.f)) m |= 1u << t;
+  }
+  return m;
+}
+
+// 256 threads, three CTAs per SM: the register budget that keeps three tiles'
+// row loads in flight per SM (the kernel waits on those loads, not on issue)
 template <int RSW>
-__global__ void __launch_bounds__(512) layer0_bits_kernel(const Layer0Args a) {
+__global__ void __launch_bounds__(256, 3) layer0_bits_kernel(const Layer0Args a) {
   extern __shared__ __align__(128) uint32_t bits[];  // RSW words
   __shared__ float s_sum[128];
+  __shared__ float s_val[128];  // output of a row with count k (scalar bias)
   __shared__ int32_t s_rows[32];
   __shared__ uint32_t s_mask;
   __shared__ int32_t s_nonbin;
@@ -44,9 +170,13 @@ __global__ void __launch_bounds__(512) layer0_bits_kernel(const Layer0Args a) {
   const int N = a.N;
   const int count = *a.count_in;
   const int n_tiles = (count + 31) / 32;
-  if (tid < 128) s_sum[tid] = a.sums[tid];
+  if (tid < 128) {
+    s_sum[tid] = a.sums[tid];
+    s_val[tid] = clampf(a.sums[tid] + a.bias, a.clampv);
+  }
   for (int i = N + tid; i < RSW; i += blockDim.x) bits[i] = 0u;
   __syncthreads();
+  const CountInterval iv = count_interval(s_sum, a.bias, a.bias_vec != nullptr);
 
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int row0 = tile * 32;
@@ -141,17 +271,8 @@ __global__ void __launch_bounds__(512) layer0_bits_kernel(const Layer0Args a) {
         t = thirtytwos & c; thirtytwos ^= c; c = t;
         sixtyfours ^= c;
       }
-      const int c_out = g * 32 + lane;
-      const float bc = a.bias_vec ? __ldg(a.bias_vec + c_out) : a.bias;
-      for (int t = 0; t < nrows; ++t) {
-        const uint32_t k = ((ones >> t) & 1u) | (((twos >> t) & 1u) << 1) |
-                           (((fours >> t) & 1u) << 2) | (((eights >> t) & 1u) << 3) |
-                           (((sixteens >> t) & 1u) << 4) | (((thirtytwos >> t) & 1u) << 5) |
-                           (((sixtyfours >> t) & 1u) << 6);
-        const float v = s_sum[k] + bc;
-        a.y_out[(size_t)s_rows[t] * N + c_out] = clampf(v, a.clampv);
-        if (__any_sync(0xffffffffu, v > 0.f)) m |= 1u << t;
-      }
+      const uint32_t P[7] = {ones, twos, fours, eights, sixteens, thirtytwos, sixtyfours};
+      m |= bits_epilogue(P, a, s_sum, s_val, iv, s_rows, nrows, g * 32 + lane, lane);
     }
     if (lane == 0 && m) atomicOr(&s_mask, m);
     __syncthreads();
@@ -288,7 +409,11 @@ __global__ void __launch_bounds__(kChunkWarps * 32) bits_count_chunked_kernel(co
   constexpr int per_item = kChunkWarps * kChunkGroupsPerWarp;
   const int subsets = (a.G + per_item - 1) / per_item;
   const long items = (long)n_tiles * subsets;
-  if (tid < 128) s_sum[tid] = a.sums[tid];
+  __shared__ float s_val[128];
+  if (tid < 128) {
+    s_sum[tid] = a.sums[tid];
+    s_val[tid] = clampf(a.sums[tid] + a.bias, a.clampv);
+  }
   for (int i = tid; i < 32; i += blockDim.x) cbits[Q + i] = 0u;
   if (tid == 0) {
     mbar_init(&bar, 1);
@@ -297,6 +422,7 @@ __global__ void __launch_bounds__(kChunkWarps * 32) bits_count_chunked_kernel(co
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
+  const CountInterval iv = count_interval(s_sum, a.bias, a.bias_vec != nullptr);
   uint32_t phase = 0;
   for (long item = blockIdx.x; item < items; item += gridDim.x) {
     const int tile = (int)(item / subsets), sub = (int)(item % subsets);
@@ -339,16 +465,7 @@ __global__ void __launch_bounds__(kChunkWarps * 32) bits_count_chunked_kernel(co
     for (int k = 0; k < kChunkGroupsPerWarp; ++k) {
       const int g = sub * per_item + k * kChunkWarps + warp;
       if (g >= a.G) continue;
-      const int c_out = g * 32 + lane;
-      const float bc = a.bias_vec ? __ldg(a.bias_vec + c_out) : a.bias;
-      for (int t = 0; t < nrows; ++t) {
-        uint32_t kk = 0;
-#pragma unroll
-        for (int i = 0; i < 7; ++i) kk |= ((c[k][i] >> t) & 1u) << i;
-        const float v = s_sum[kk] + bc;
-        a.y_out[(size_t)s_rows[t] * N + c_out] = clampf(v, a.clampv);
-        if (__any_sync(0xffffffffu, v > 0.f)) m |= 1u << t;
-      }
+      m |= bits_epilogue(c[k], a, s_sum, s_val, iv, s_rows, nrows, g * 32 + lane, lane);
     }
     if (lane == 0 && m) atomicOr(&s_mask, m);
     __syncthreads();
