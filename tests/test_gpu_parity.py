@@ -476,3 +476,29 @@ def test_bounded_wait_times_out_and_engine_stays_usable():
         flags, ids = eng.infer(Y0)
     _, alive, _ = orc.infer(_layers(N, L, seed), N, -0.3, Y0, precision=64, want_y=False)
     assert np.array_equal(flags, alive)
+
+
+@pytest.mark.parametrize("N,L,T", [(1024, 40, 20), (4096, 40, 20), (65536, 33, 30)])
+def test_chain_with_several_centroids(N, L, T):
+    """Rows that are copies of a few prototypes: merging leaves one row per
+    prototype, the clustering keeps them as centroids without residues, and a
+    chain launch carries several rows at once (cluster or grid kernel); the
+    result must match the per-layer launches bitwise and the oracle."""
+    seed = 13
+    protos = sg.generate_inputs(N, seed, 0, 40)
+    bias = sg.load().sdnn_reference_bias(N)
+    Y0 = protos[np.arange(48) % 40]
+    out = {}
+    for chain in (True, False):
+        with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=48, bias=bias, num_centroids=50,
+                       chain=chain, merge_start=1) as eng:
+            eng.generate_weights(seed)
+            flags, ids = eng.infer(Y0)
+            out[chain] = (flags, ids, eng.activations(48), eng.stats())
+    st = out[True][3]
+    if st["residue_rows"] == 0 and st["centroids"] > 1:
+        assert st["post_kernel"] in (2, 3, 4), st
+    assert np.array_equal(out[True][1], out[False][1])
+    assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
+    Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
+    _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"K chain N={N}", Y32=Y32)
