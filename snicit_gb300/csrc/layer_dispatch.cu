@@ -5,6 +5,11 @@
 
 namespace sdnn {
 
+#ifndef SDNN_LAYER_PDL
+#define SDNN_LAYER_PDL 1
+#endif
+constexpr bool kLayerPdl = SDNN_LAYER_PDL;
+
 void register_layer_q1024(std::vector<LayerInstance>& v);
 void register_layer_q4096(std::vector<LayerInstance>& v);
 void register_layer_q16384(std::vector<LayerInstance>& v);
@@ -56,8 +61,21 @@ cudaError_t launch_layer(const LayerKernelKey& key, const LayerArgs& a, int grid
                          size_t smem, cudaStream_t s) {
   const LayerInstance* e = find(key);
   if (!e) return cudaErrorInvalidValue;
+  // programmatic stream serialization: this launch may be scheduled while the
+  // previous kernel on the stream finishes (the kernel waits for it with
+  // griddepcontrol.wait before touching its outputs)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = kLayerPdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   void* args[] = {const_cast<LayerArgs*>(&a)};
-  return cudaLaunchKernel(e->fn, dim3(grid), dim3(threads), args, smem, s);
+  return cudaLaunchKernelExC(&cfg, e->fn, args);
 }
 
 }  // namespace sdnn

@@ -337,8 +337,11 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int RS = RSW > 0 ? RSW : a.Q + 32;
-  const Split sp = make_split<T>(a);
-  if (sp.count <= 0 || (long)blockIdx.x >= sp.items) return;
+  // Launched with programmatic stream serialization: the next launch may be
+  // scheduled now, and this one may have started before its predecessor
+  // ended -- so only CTA-local setup comes before griddepcontrol.wait, which
+  // returns once the predecessor has completed and its writes are visible.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   // One tile buffer, reloaded per item (and input chunk): the load of one CTA
   // overlaps the compute of the other CTAs on the SM (up to four).
   for (int i = tid; i < T * 32; i += blockDim.x) ys[(i >> 5) * RS + a.Q + (i & 31)] = 0.f;
@@ -349,6 +352,9 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const Split sp = make_split<T>(a);
+  if (sp.count <= 0 || (long)blockIdx.x >= sp.items) return;
   __syncthreads();
 
   if constexpr (KG == 1) {
