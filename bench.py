@@ -306,18 +306,33 @@ def run_ours(args):
     host_t = torch.empty((B, N), dtype=torch.float32, pin_memory=True)
     host_t.copy_(d_in)
     host = host_t.numpy()
-    eng.infer(host, want_flags=False, want_ids=True)
-    e2e_t = []
-    count = 0
-    for _ in range(max(1, min(args.steps, 10))):
-        t0 = time.perf_counter()
-        _, ids = eng.infer(host, want_flags=False, want_ids=True)
-        e2e_t.append(time.perf_counter() - t0)
-        count = len(ids)
+
+    def time_host_calls():
+        eng.infer(host, want_flags=False, want_ids=True)
+        times, n = [], 0
+        for _ in range(max(1, min(args.steps, 10))):
+            t0 = time.perf_counter()
+            _, ids = eng.infer(host, want_flags=False, want_ids=True)
+            times.append(time.perf_counter() - t0)
+            n = len(ids)
+        return statistics.median(times), n
+
+    # streamed ingest (the default): the rows copy in pieces and the layers
+    # before the first merge run on each piece while the next ones copy
+    e2e_s, count = time_host_calls()
+    pieces = eng.stats()["input_pieces"]
     assert count == int(flags.sum())
-    e2e_s = statistics.median(e2e_t)
     e2e = {"value": world * edges / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": B * N * 4,
-           "d2h_bytes_per_step": 4 + 4 * count, "ms_per_step": e2e_s * 1e3}
+           "d2h_bytes_per_step": 4 + 4 * count, "ms_per_step": e2e_s * 1e3,
+           "input_pieces": pieces}
+    # the same call with one copy of the whole batch before the first layer
+    eng.set_input_streaming(-1)
+    one_s, count1 = time_host_calls()
+    eng.set_input_streaming(0)
+    assert count1 == count
+    e2e_one_copy = {"value": world * edges / one_s, "unit": "edges/s",
+                    "h2d_bytes_per_step": B * N * 4, "d2h_bytes_per_step": 4 + 4 * count,
+                    "ms_per_step": one_s * 1e3}
     # the same with the inputs as one-bit host rows (the inputs are 0/1): 32x fewer bytes
     bits_t = torch.from_numpy(sg.pack_bits(host)).pin_memory()
     bits = bits_t.numpy()
@@ -381,7 +396,7 @@ def run_ours(args):
             "plain": {"ms_per_inference": plain_ms, "edges_per_s": edges / (plain_ms / 1e3),
                       "category_set_equal": plain_exact, "row_layers": pst["row_layers"]},
             "speedup_vs_plain": plain_ms / ms_per_step,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "e2e_bit_inputs": e2e_bits,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "e2e_one_copy": e2e_one_copy, "e2e_bit_inputs": e2e_bits,
             "gpu_launches": st["launches"] * args.steps,
             "clocks": clk.summary(),
         }

@@ -78,7 +78,9 @@ typedef struct sdnn_config {
   int32_t merge_start;   /* SNICIT: first plain layer after which identical rows
                             are merged (0 = automatic)                            */
   int32_t merge_every;   /* ... and then after every merge_every-th layer (0 = 1)  */
-  int32_t reserved[2];
+  int32_t input_piece_rows; /* host FP32 inputs: rows per copy piece of the streamed
+                            ingest (0 = automatic, 8192)                          */
+  int32_t reserved[1];
 } sdnn_config;
 
 /* sdnn_config.flags: switch off layout optimisations (results are identical
@@ -95,6 +97,8 @@ typedef struct sdnn_config {
                                            /* of streaming them into shared memory        */
 #define SDNN_FLAG_NO_GRID_CHAIN 32         /* no grid-wide chain: the cluster chain (or    */
                                            /* per-layer launches where it cannot run)     */
+#define SDNN_FLAG_NO_STREAMED_INPUT 64     /* host FP32 inputs: one copy of the whole batch */
+                                           /* before the first layer (no piecewise ingest) */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -110,7 +114,9 @@ typedef struct sdnn_stats {
   int32_t threshold;     /* threshold layer used                               */
   int32_t tile_rows;     /* tile rows used by the layer kernel                 */
   int32_t threads;       /* threads per CTA used by the layer kernel           */
-  int32_t reserved0;
+  int32_t input_pieces;  /* host FP32 inputs: copy pieces of the last call (the
+                            layers before the first cross-row step ran per piece
+                            while later pieces were copied); 0 = not streamed     */
   int64_t pre_row_layers;   /* rows processed by the plain layers (sum)        */
   int64_t post_row_layers;  /* centroid + residue rows of the post layers      */
   int64_t weight_nnz;       /* nonzeros of all L layers                        */
@@ -244,6 +250,14 @@ int sdnn_selftest_wait_timeout(sdnn_engine* e, int64_t limit_us);
  * weights, e.g. to time the plain path and SNICIT on one resident copy of W.
  * (The reference picks the engine class once, main/SDGC.cu:104-110.) */
 int sdnn_set_mode(sdnn_engine* e, int32_t mode, int32_t threshold);
+
+/* Streamed ingest of host FP32 rows (sdnn_infer_host): piece_rows > 0 copies
+ * the rows in pieces of that many rows and runs the layers before the first
+ * cross-row step on each piece while the next ones copy; 0 = automatic piece
+ * size; < 0 = one copy of the whole batch before the first layer.  Results
+ * are bitwise the same either way.  (The reference reads the whole input
+ * before its first layer, src/SDGC/SNICIT/SNICIT.hpp:298.) */
+int sdnn_set_input_streaming(sdnn_engine* e, int32_t piece_rows);
 
 /* Rows processed by every layer of the last inference (plain rows for layers
  * below the threshold -- one per set of merged identical rows in SNICIT mode

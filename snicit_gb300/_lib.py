@@ -16,6 +16,7 @@ FLAG_NO_CHAIN = 4
 FLAG_NO_MERGE = 8
 FLAG_NO_CHAIN_STREAM = 16
 FLAG_NO_GRID_CHAIN = 32
+FLAG_NO_STREAMED_INPUT = 64
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",
@@ -38,7 +39,8 @@ class Config(ctypes.Structure):
         ("autotune", ctypes.c_int32), ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
         ("tile_rows", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("flags", ctypes.c_int32), ("merge_start", ctypes.c_int32),
-        ("merge_every", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
+        ("merge_every", ctypes.c_int32), ("input_piece_rows", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 1),
     ]
 
 
@@ -49,7 +51,7 @@ class Stats(ctypes.Structure):
         ("row_layers", ctypes.c_int64), ("centroids", ctypes.c_int32),
         ("residue_rows", ctypes.c_int32), ("launches", ctypes.c_int32),
         ("threshold", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
-        ("threads", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+        ("threads", ctypes.c_int32), ("input_pieces", ctypes.c_int32),
         ("pre_row_layers", ctypes.c_int64), ("post_row_layers", ctypes.c_int64),
         ("weight_nnz", ctypes.c_int64), ("centroid_candidates", ctypes.c_int32),
         ("merge_start", ctypes.c_int32), ("merge_every", ctypes.c_int32),
@@ -102,6 +104,7 @@ SIGNATURES = [
     ("sdnn_autotune", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_autotune_device", ctypes.c_int, [P, P, I64, ctypes.c_char_p]),
     ("sdnn_set_mode", ctypes.c_int, [P, I32, I32]),
+    ("sdnn_set_input_streaming", ctypes.c_int, [P, I32]),
     ("sdnn_selftest_wait_timeout", ctypes.c_int, [P, I64]),
     ("sdnn_save_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_load_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),

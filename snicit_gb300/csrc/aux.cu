@@ -34,6 +34,19 @@ void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s) {
 __global__ void set_scalar_kernel(int32_t* p, int32_t v) { *p = v; }
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s) { set_scalar_kernel<<<1, 1, 0, s>>>(p, v); }
 
+__global__ void sum_piece_counts_kernel(const int32_t* pc, int pieces, int stride, int layers,
+                                        int32_t* counts) {
+  for (int l = threadIdx.x; l < layers; l += blockDim.x) {
+    int32_t t = 0;
+    for (int p = 0; p < pieces; ++p) t += pc[(size_t)p * stride + l];
+    counts[l] = t;
+  }
+}
+void launch_sum_piece_counts(const int32_t* piece_counts, int pieces, int stride, int layers,
+                             int32_t* counts, cudaStream_t s) {
+  sum_piece_counts_kernel<<<1, 256, 0, s>>>(piece_counts, pieces, stride, layers, counts);
+}
+
 __global__ void begin_rows_kernel(const int32_t* nrows, int32_t* list, int32_t* count,
                                   int32_t* zero_a, int32_t* zero_b, int32_t* neg) {
   const int n = *nrows;

@@ -51,10 +51,11 @@ struct GraphKey {
   int64_t rows = -1;
   const float* in = nullptr;
   int32_t* flags = nullptr;
-  int T = -1, K = -1, mode = -1, tile = -1, threads = -1, chain_kc = -1;
+  int T = -1, K = -1, mode = -1, tile = -1, threads = -1, chain_kc = -1, start = -1;
   bool operator==(const GraphKey& o) const {
     return rows == o.rows && in == o.in && flags == o.flags && T == o.T && K == o.K &&
-           mode == o.mode && tile == o.tile && threads == o.threads && chain_kc == o.chain_kc;
+           mode == o.mode && tile == o.tile && threads == o.threads && chain_kc == o.chain_kc &&
+           start == o.start;
   }
 };
 
@@ -63,6 +64,10 @@ struct GraphSlot {
   GraphKey key;
   int launches = 0;
 };
+
+// Streamed ingest of host FP32 rows: at most this many copy pieces per call.
+constexpr int kMaxPieces = 16;
+constexpr int kDefaultPieceRows = 8192;
 
 struct GenSpec {
   bool on = false;
@@ -146,8 +151,27 @@ struct sdnn_engine {
 
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
-  // graph cache: one captured graph per phase of an inference
-  GraphSlot graphs[5];
+  // streamed ingest of host FP32 rows: a copy stream, one event per piece and
+  // the per-piece row counts of the layers run piece by piece
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t piece_ev[kMaxPieces] = {};
+  cudaEvent_t ingest_free = nullptr, lane_ev = nullptr;
+  // second lane for odd pieces: its own stream, tile tickets and layer-0
+  // fallback list (swapped in with swap_lane), so one piece's layers fill the
+  // last partial wave of the other's
+  cudaStream_t stream2 = nullptr;
+  uint32_t* d_tmask2 = nullptr;
+  int32_t* d_ticket2 = nullptr;
+  int32_t* d_fallback2 = nullptr;
+  int32_t* d_fbcount2 = nullptr;
+  int32_t* d_pcounts = nullptr;  // [kMaxPieces][L + 2]
+  int32_t* d_plist[2] = {nullptr, nullptr};  // [cap] row lists of the pieces' layers
+  int pipe_start = 0;            // first layer of the graphed part (0: every layer)
+  int last_pieces = 0;
+
+  // graph cache: one captured graph per phase of an inference (slots 5 and 6:
+  // PH_ALL and PH_PRE starting after the layers run piece by piece)
+  GraphSlot graphs[7];
   int run_launches = 0;
   int32_t* h_counts = nullptr;  // pinned: residue rows and centroids after clustering
   int chain_cap = 0;            // centroid rows the cluster chain kernel can carry
@@ -242,6 +266,13 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_mpos);
   dfree(e->d_mtmp);
   dfree(e->d_mcount);
+  dfree(e->d_pcounts);
+  dfree(e->d_plist[0]);
+  dfree(e->d_plist[1]);
+  dfree(e->d_tmask2);
+  dfree(e->d_ticket2);
+  dfree(e->d_fallback2);
+  dfree(e->d_fbcount2);
   if (e->h_counts) cudaFreeHost(e->h_counts);
   e->h_counts = nullptr;
   e->cap = 0;
@@ -390,6 +421,13 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   }
   T(A(&e->d_fbcount, 16));
   T(A(&e->d_rows, 16));
+  T(A(&e->d_pcounts, (size_t)kMaxPieces * (e->L + 2) * 4));
+  T(A(&e->d_plist[0], (size_t)cap * 4));
+  T(A(&e->d_plist[1], (size_t)cap * 4));
+  T(A(&e->d_tmask2, (size_t)(cap + 1) * 4));
+  T(A(&e->d_ticket2, (size_t)(cap + 1) * 4));
+  T(A(&e->d_fallback2, (size_t)cap * 4));
+  T(A(&e->d_fbcount2, 16));
   if (rc == cudaSuccess) T(cudaMallocHost((void**)&e->h_counts, 16));
   if (rc != cudaSuccess) {
     free_buffers(e);
@@ -399,6 +437,8 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   e->cap = cap;
   CK(cudaMemsetAsync(e->d_tmask, 0, (size_t)(cap + 1) * 4, e->stream));
   CK(cudaMemsetAsync(e->d_ticket, 0, (size_t)(cap + 1) * 4, e->stream));
+  CK(cudaMemsetAsync(e->d_tmask2, 0, (size_t)(cap + 1) * 4, e->stream));
+  CK(cudaMemsetAsync(e->d_ticket2, 0, (size_t)(cap + 1) * 4, e->stream));
   CK(cudaMemsetAsync(e->d_err, 0, 16, e->stream));
   return SDNN_OK;
 }
@@ -764,84 +804,100 @@ int enqueue_merge(sdnn_engine* e, int l) {
   return SDNN_OK;
 }
 
-int enqueue_plain_layers(sdnn_engine* e, int64_t rows, const float* d_in, int T, bool capturing) {
-  const int L = e->L;
+// Enqueues plain layer l over the row list (lin, cin) into (lout, cout);
+// layer 0 of 0/1 inputs takes the binary counting kernels, with the tiles that
+// hold other values sent to the float kernel.
+int enqueue_layer(sdnn_engine* e, int l, const float* in, const int32_t* lin, const int32_t* cin,
+                  int32_t* lout, int32_t* cout) {
   const cudaStream_t s = e->stream;
+  const bool bits = l == 0 && e->dl[0].sums && (e->bits_chunked || e->bits_grid > 0);
+  if (!bits) return layer_launch(e, l, EPI_PLAIN, in, e->d_y[l & 1], lin, cin, lout, cout);
+  CK(cudaMemsetAsync(e->d_fbcount, 0, 16, s));
+  Layer0Args b{};
+  b.idx = e->dl[0].idx;
+  b.grp_blk = e->dl[0].grp;
+  b.bias_vec = e->dl[0].bias;
+  b.bias = e->cfg.bias;
+  b.clampv = e->cfg.clamp;
+  b.sums = e->dl[0].sums;
+  b.y_in = in;
+  b.y_out = e->d_y[0];
+  b.list_in = lin;
+  b.count_in = cin;
+  b.list_out = lout;
+  b.count_out = cout;
+  b.fallback_list = e->d_fallback;
+  b.fallback_count = e->d_fbcount;
+  b.N = e->N;
+  b.G = e->G;
+  if (e->bits_chunked) {
+    // input chunks: transpose pass + counting pass
+    b.nq = e->nq;
+    b.Q = e->Q;
+    b.bits = e->d_bits;
+    b.tile_state = e->d_tile_state;
+    b.tile_mask = e->d_tmask;
+    b.tile_ticket = e->d_ticket;
+    b.err = e->d_err;
+    CK(launch_layer0_bits_chunked(b, e->num_sms, s));
+    e->launches += 2;
+  } else {
+    CK(launch_layer0_bits(b, e->bits_grid, kBitsThreads, s));
+    e->launches++;
+  }
+  return layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount, lout, cout);
+}
+
+// Enqueues plain layers e->pipe_start .. T - 1 over the global row lists (the
+// layers below pipe_start ran piece by piece, enqueue_piece), with the merge
+// steps between them.
+int enqueue_plain_layers(sdnn_engine* e, const float* d_in, int T, bool capturing) {
+  const int L = e->L;
   int rc;
   // XY mode splits the plain loop at the threshold for its pre/post timing
   // (src/SDGC/XY/XY.hpp:492-501); BF and SNIG time the loop as one stage.
   const int split = e->cfg.mode == SDNN_MODE_XY ? std::max(0, std::min(e->cfg.threshold, L)) : T;
-  for (int l = 0; l < T; ++l) {
+  const int first = e->pipe_start;
+  if (first > 0 && merge_after(e, first - 1, T) && (rc = enqueue_merge(e, first - 1))) return rc;
+  for (int l = first; l < T; ++l) {
     if (l == split && T == L) {
       if ((rc = record(e, 1, capturing))) return rc;
       if ((rc = record(e, 2, capturing))) return rc;
     }
     const float* in = l == 0 ? d_in : e->d_y[(l - 1) & 1];
-    if (l == 0 && e->dl[0].sums && e->bits_chunked) {
-      // binary inputs, input chunks: transpose pass + counting pass
-      CK(cudaMemsetAsync(e->d_fbcount, 0, 16, s));
-      Layer0Args b{};
-      b.idx = e->dl[0].idx;
-      b.grp_blk = e->dl[0].grp;
-      b.bias_vec = e->dl[0].bias;
-      b.bias = e->cfg.bias;
-      b.clampv = e->cfg.clamp;
-      b.sums = e->dl[0].sums;
-      b.y_in = in;
-      b.y_out = e->d_y[0];
-      b.list_in = e->d_list[0];
-      b.count_in = e->d_counts;
-      b.list_out = e->d_list[1];
-      b.count_out = e->d_counts + 1;
-      b.fallback_list = e->d_fallback;
-      b.fallback_count = e->d_fbcount;
-      b.N = e->N;
-      b.G = e->G;
-      b.nq = e->nq;
-      b.Q = e->Q;
-      b.bits = e->d_bits;
-      b.tile_state = e->d_tile_state;
-      b.tile_mask = e->d_tmask;
-      b.tile_ticket = e->d_ticket;
-      b.err = e->d_err;
-      CK(launch_layer0_bits_chunked(b, e->num_sms, s));
-      e->launches += 2;
-      if ((rc = layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount,
-                             e->d_list[1], e->d_counts + 1)))
-        return rc;
-    } else if (l == 0 && e->dl[0].sums && e->bits_grid > 0) {
-      // binary inputs: counting kernel; tiles with other values go to the float kernel
-      CK(cudaMemsetAsync(e->d_fbcount, 0, 16, s));
-      Layer0Args b{};
-      b.idx = e->dl[0].idx;
-      b.grp_blk = e->dl[0].grp;
-      b.bias_vec = e->dl[0].bias;
-      b.bias = e->cfg.bias;
-      b.clampv = e->cfg.clamp;
-      b.sums = e->dl[0].sums;
-      b.y_in = in;
-      b.y_out = e->d_y[0];
-      b.list_in = e->d_list[0];
-      b.count_in = e->d_counts;
-      b.list_out = e->d_list[1];
-      b.count_out = e->d_counts + 1;
-      b.fallback_list = e->d_fallback;
-      b.fallback_count = e->d_fbcount;
-      b.N = e->N;
-      b.G = e->G;
-      CK(launch_layer0_bits(b, e->bits_grid, kBitsThreads, s));
-      e->launches++;
-      if ((rc = layer_launch(e, 0, EPI_PLAIN, in, e->d_y[0], e->d_fallback, e->d_fbcount,
-                             e->d_list[1], e->d_counts + 1)))
-        return rc;
-    } else if ((rc = layer_launch(e, l, EPI_PLAIN, in, e->d_y[l & 1], e->d_list[l & 1],
-                                  e->d_counts + l, e->d_list[(l + 1) & 1], e->d_counts + l + 1))) {
+    if ((rc = enqueue_layer(e, l, in, e->d_list[l & 1], e->d_counts + l, e->d_list[(l + 1) & 1],
+                            e->d_counts + l + 1)))
       return rc;
-    }
     if (merge_after(e, l, T) && (rc = enqueue_merge(e, l))) return rc;
   }
   if (!(split < T && T == L)) {
     if ((rc = record(e, 1, capturing))) return rc;
+  }
+  return SDNN_OK;
+}
+
+// Layers 0 .. m - 1 of one piece of rows (rows r0 .. r0 + n - 1 of the batch),
+// enqueued eagerly once the piece's copy has landed.  Rows are independent
+// until the first cross-row step (the first merge or the threshold
+// clustering), so every row gets the same bits as in the whole-batch run.
+// The piece keeps its row lists in its own segment [r0, r0 + n) of the piece
+// list buffers (d_plist, identity rows for layer 0) with its own counters; its
+// last layer appends the survivors to the global list of layer m, which no
+// piece list shares memory with.
+int enqueue_piece(sdnn_engine* e, int p, int64_t r0, int64_t n, int m, const float* d_in) {
+  int32_t* pc = e->d_pcounts + (size_t)p * (e->L + 2);
+  // an ordinary launch right after the copy's event: the layer launches that
+  // follow (programmatic serialization) then wait for a completed kernel
+  launch_set_scalar(pc, (int32_t)n, e->stream);
+  e->launches++;
+  CK(cudaGetLastError());
+  for (int l = 0; l < m; ++l) {
+    const float* in = l == 0 ? d_in : e->d_y[(l - 1) & 1];
+    const bool last = l + 1 == m;
+    int32_t* lout = last ? e->d_list[m & 1] : e->d_plist[(l + 1) & 1] + r0;
+    int32_t* cout = last ? e->d_counts + m : pc + l + 1;
+    int rc = enqueue_layer(e, l, in, e->d_plist[l & 1] + r0, pc + l, lout, cout);
+    if (rc) return rc;
   }
   return SDNN_OK;
 }
@@ -858,11 +914,13 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
   const int32_t* live_count = e->d_counts + T;
   (void)rows;  // the row count is read on the device from d_rows
   if (phase == PH_ALL || phase == PH_PRE) {
-    if ((rc = record(e, 0, capturing))) return rc;
-    CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
-    launch_begin_rows(e->d_rows, e->d_list[0], e->d_counts, d_flags, e->d_state, e->d_alias, s);
-    e->launches++;
-    if ((rc = enqueue_plain_layers(e, rows, d_in, T, capturing))) return rc;
+    if (e->pipe_start == 0) {
+      if ((rc = record(e, 0, capturing))) return rc;
+      CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(L + 4) * 4, s));
+      launch_begin_rows(e->d_rows, e->d_list[0], e->d_counts, d_flags, e->d_state, e->d_alias, s);
+      e->launches++;
+    }
+    if ((rc = enqueue_plain_layers(e, d_in, T, capturing))) return rc;
   }
   if (phase == PH_PRE) {
     if (T == 0) {
@@ -992,10 +1050,12 @@ int run_phase(sdnn_engine* e, int slot, int phase, int64_t rows, const float* d_
     e->launches = before;
     return rc;
   }
-  GraphSlot& g = e->graphs[slot];
+  const bool streamed = e->pipe_start > 0 && (phase == PH_ALL || phase == PH_PRE);
+  GraphSlot& g = e->graphs[streamed ? 5 + slot : slot];
   const GraphKey key{0, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
                      e->key.T, e->threads,
-                     phase == PH_POST_CHAIN ? e->chain_kc * 4 + e->chain_kind : 0};
+                     phase == PH_POST_CHAIN ? e->chain_kc * 4 + e->chain_kind : 0,
+                     streamed ? e->pipe_start : 0};
   if (!g.exec || !(g.key == key)) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g.exec = nullptr;
@@ -1031,6 +1091,7 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   e->last_T = T;
   e->last_rows = rows;
   e->run_launches = 0;
+  if (e->pipe_start == 0) e->last_pieces = 0;
   // the graphs read the row count from d_rows (one graph for every count)
   launch_set_scalar(e->d_rows, (int32_t)rows, e->stream);
   e->run_launches++;
@@ -1164,6 +1225,7 @@ int collect_stats(sdnn_engine* e) {
   st.threshold = T;
   st.tile_rows = e->key.T;
   st.threads = e->threads;
+  st.input_pieces = e->last_pieces;
   st.centroid_candidates = e->cfg.num_centroids;
   st.merge_start = merging_on(e) ? (e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart) : 0;
   st.merge_every = merging_on(e) ? std::max(1, e->cfg.merge_every) : 0;
@@ -1258,6 +1320,12 @@ int sdnn_destroy(sdnn_engine* e) {
   free_buffers(e);
   for (auto& ev : e->ev)
     if (ev) cudaEventDestroy(ev);
+  for (auto& ev : e->piece_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (e->ingest_free) cudaEventDestroy(e->ingest_free);
+  if (e->lane_ev) cudaEventDestroy(e->lane_ev);
+  if (e->copy_stream) cudaStreamDestroy(e->copy_stream);
+  if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return SDNN_OK;
@@ -1355,6 +1423,104 @@ int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows, int32_t* 
   return rc;
 }
 
+// First layer of the cross-row part of an inference (the first merge step in
+// SNICIT mode, else the threshold clustering; L in SNIG mode): the layers
+// before it may run piece by piece.  0 when host inputs are not streamed.
+int streamed_prefix(const sdnn_engine* e) {
+  if (e->cfg.flags & SDNN_FLAG_NO_STREAMED_INPUT) return 0;
+  if (e->cfg.mode != SDNN_MODE_SNIG && e->cfg.mode != SDNN_MODE_SNICIT) return 0;
+  const int T = effective_threshold(e);
+  int m = T;
+  if (merging_on(e)) {
+    const int start = e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart;
+    if (start < T) m = std::min(m, start);
+  }
+  return m;
+}
+
+// Swaps the engine's stream, tile tickets and layer-0 fallback list with the
+// second lane's (called in pairs around the work of an odd piece).
+void swap_lane(sdnn_engine* e) {
+  std::swap(e->stream, e->stream2);
+  std::swap(e->d_tmask, e->d_tmask2);
+  std::swap(e->d_ticket, e->d_ticket2);
+  std::swap(e->d_fallback, e->d_fallback2);
+  std::swap(e->d_fbcount, e->d_fbcount2);
+}
+
+// One inference of n host FP32 rows with the copy streamed in P pieces: the
+// pieces are copied back to back on the copy stream, and the compute lanes
+// (even and odd pieces) run layers 0 .. m - 1 of piece p as soon as its copy
+// has landed (while the later pieces are still copying), then the rest of the
+// inference from layer m over all rows (the graphed phases with pipe_start = m).
+int run_streamed(sdnn_engine* e, const float* Y0, int64_t n, int m, int P) {
+  const int64_t N = e->N;
+  const cudaStream_t s = e->stream;
+  if (!e->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&e->ingest_free, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&e->lane_ev, cudaEventDisableTiming));
+    for (auto& ev : e->piece_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  // the copies overwrite d_in: only after everything enqueued so far
+  CK(cudaEventRecord(e->ingest_free, s));
+  CK(cudaStreamWaitEvent(e->copy_stream, e->ingest_free, 0));
+  int64_t bnd[kMaxPieces + 1];
+  for (int p = 0; p <= P; ++p)  // piece boundaries on 32-row tiles
+    bnd[p] = p == P ? n : std::min<int64_t>(n, (n * p / P + 31) / 32 * 32);
+  for (int p = 0; p < P; ++p) {
+    const int64_t rows = bnd[p + 1] - bnd[p];
+    if (rows > 0)
+      CK(cudaMemcpyAsync(e->d_in + bnd[p] * N, Y0 + bnd[p] * N, (size_t)(rows * N) * 4,
+                         cudaMemcpyHostToDevice, e->copy_stream));
+    CK(cudaEventRecord(e->piece_ev[p], e->copy_stream));
+  }
+  e->launches = 0;
+  int rc;
+  if ((rc = record(e, 0, false))) return rc;
+  launch_set_scalar(e->d_rows, (int32_t)n, s);
+  CK(cudaMemsetAsync(e->d_counts, 0, (size_t)(e->L + 4) * 4, s));
+  CK(cudaMemsetAsync(e->d_pcounts, 0, (size_t)P * (e->L + 2) * 4, s));  // the layers append
+  // identity rows into the pieces' layer-0 lists
+  launch_begin_rows(e->d_rows, e->d_plist[0], e->d_counts, e->d_flags, e->d_state, e->d_alias, s);
+  e->launches += 2;
+  // two lanes (the chunked binary layer 0 has one set of bit buffers: one lane)
+  const bool two = !e->bits_chunked;
+  if (two) {
+    CK(cudaEventRecord(e->lane_ev, s));
+    CK(cudaStreamWaitEvent(e->stream2, e->lane_ev, 0));
+  }
+  // Pieces of different lanes run at the same time: their rows, list segments
+  // and counters are disjoint, and both append to the global list of layer m
+  // with atomics.
+  for (int p = 0; p < P; ++p) {
+    const bool odd = two && (p & 1);
+    if (odd) swap_lane(e);
+    rc = SDNN_OK;
+    const cudaError_t w = cudaStreamWaitEvent(e->stream, e->piece_ev[p], 0);
+    if (w == cudaSuccess) rc = enqueue_piece(e, p, bnd[p], bnd[p + 1] - bnd[p], m, e->d_in);
+    if (odd) swap_lane(e);
+    if (w != cudaSuccess) return cuda_fail(e, w, "cudaStreamWaitEvent");
+    if (rc) return rc;
+  }
+  if (two) {
+    CK(cudaEventRecord(e->lane_ev, e->stream2));
+    CK(cudaStreamWaitEvent(s, e->lane_ev, 0));
+  }
+  launch_sum_piece_counts(e->d_pcounts, P, e->L + 2, m, e->d_counts, s);
+  e->launches++;
+  CK(cudaGetLastError());
+  const int prefix_launches = e->launches;
+  e->pipe_start = m;
+  e->last_pieces = P;
+  rc = run(e, n, e->d_in, e->d_flags);
+  e->pipe_start = 0;
+  if (rc) return rc;
+  e->launches += prefix_launches;  // run() counted its own launches only
+  return SDNN_OK;
+}
+
 // Host inference over batches of cfg.batch rows; inputs as FP32 rows, or as
 // one-bit rows (bits != nullptr) expanded on the device.
 int infer_host(sdnn_engine* e, const float* Y0, const uint64_t* bits, int64_t rows, int32_t* flags,
@@ -1370,18 +1536,25 @@ int infer_host(sdnn_engine* e, const float* Y0, const uint64_t* bits, int64_t ro
   }
   int64_t total = 0;
   sdnn_stats acc{};
+  const int m = bits ? 0 : streamed_prefix(e);
+  const int64_t piece_rows =
+      e->cfg.input_piece_rows > 0 ? e->cfg.input_piece_rows : kDefaultPieceRows;
   for (int64_t off = 0; off < rows; off += e->cfg.batch) {
     const int64_t n = std::min<int64_t>(e->cfg.batch, rows - off);
+    const int P = m > 0 ? (int)std::min<int64_t>(kMaxPieces, (n + piece_rows - 1) / piece_rows) : 1;
     if (bits) {
       CK(cudaMemcpyAsync(e->d_inbits, bits + off * W, (size_t)(n * W) * 8, cudaMemcpyHostToDevice,
                          e->stream));
       launch_expand_bits(e->d_inbits, n, e->N, e->d_in, e->stream);
       CK(cudaGetLastError());
+      rc = run(e, n, e->d_in, e->d_flags);
+    } else if (P > 1) {
+      rc = run_streamed(e, Y0 + off * N, n, m, P);
     } else {
       CK(cudaMemcpyAsync(e->d_in, Y0 + off * N, (size_t)(n * N) * 4, cudaMemcpyHostToDevice,
                          e->stream));
+      rc = run(e, n, e->d_in, e->d_flags);
     }
-    rc = run(e, n, e->d_in, e->d_flags);
     if (rc) return rc;
     if (ids || count) {
       launch_flags_to_ids(e->d_flags, (int32_t)n, e->d_ids, e->d_idcount, e->stream);
@@ -1629,6 +1802,17 @@ int sdnn_set_mode(sdnn_engine* e, int32_t mode, int32_t threshold) {
   e->cfg.mode = mode;
   e->cfg.threshold = threshold;
   drop_graph(e);
+  return SDNN_OK;
+}
+
+int sdnn_set_input_streaming(sdnn_engine* e, int32_t piece_rows) {
+  if (!e) return SDNN_ERR_INVALID;
+  if (piece_rows < 0) {
+    e->cfg.flags |= SDNN_FLAG_NO_STREAMED_INPUT;
+  } else {
+    e->cfg.flags &= ~SDNN_FLAG_NO_STREAMED_INPUT;
+    e->cfg.input_piece_rows = piece_rows;
+  }
   return SDNN_OK;
 }
 

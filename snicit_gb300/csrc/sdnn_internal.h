@@ -163,6 +163,10 @@ cudaError_t launch_grid_chain(const GridChainArgs& a, int kc_needed, int num_sms
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s);
+// counts[l] = sum over pieces p of piece_counts[p * stride + l], l < layers
+// (row counts of the layers run piece by piece).
+void launch_sum_piece_counts(const int32_t* piece_counts, int pieces, int stride, int layers,
+                             int32_t* counts, cudaStream_t s);
 // list[i] = i, zero_a[i] = zero_b[i] = 0 and neg[i] = -1 for i < *nrows;
 // *count = *nrows
 void launch_begin_rows(const int32_t* nrows, int32_t* list, int32_t* count, int32_t* zero_a,

@@ -23,7 +23,7 @@ class Engine:
                  batch=60000, bias=None, clamp=32.0, num_centroids=32, seed=20260101,
                  device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
                  chain=True, merge=True, merge_start=0, merge_every=0, chain_stream=True,
-                 grid_chain=True):
+                 grid_chain=True, streamed_input=True, input_piece_rows=0):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -44,9 +44,11 @@ class Engine:
                      | (0 if chain else _lib.FLAG_NO_CHAIN)
                 | (0 if merge else _lib.FLAG_NO_MERGE)
                 | (0 if chain_stream else _lib.FLAG_NO_CHAIN_STREAM)
-                | (0 if grid_chain else _lib.FLAG_NO_GRID_CHAIN))
+                | (0 if grid_chain else _lib.FLAG_NO_GRID_CHAIN)
+                | (0 if streamed_input else _lib.FLAG_NO_STREAMED_INPUT))
         cfg.merge_start = int(merge_start)
         cfg.merge_every = int(merge_every)
+        cfg.input_piece_rows = int(input_piece_rows)
         self.cfg = cfg
         self.N = cfg.num_neurons
         self.L = cfg.num_layers
@@ -171,7 +173,7 @@ class Engine:
             "pre_row_layers": s.pre_row_layers, "post_row_layers": s.post_row_layers,
             "weight_nnz": s.weight_nnz, "centroid_candidates": s.centroid_candidates,
             "merge_start": s.merge_start, "merge_every": s.merge_every,
-            "post_kernel": s.post_kernel,
+            "post_kernel": s.post_kernel, "input_pieces": s.input_pieces,
         }
 
     def layer_rows(self):
@@ -194,6 +196,11 @@ class Engine:
         self._ck(load().sdnn_set_mode(self._h, m, t))
         self.cfg.mode = m
         self.cfg.threshold = t
+
+    def set_input_streaming(self, piece_rows):
+        """Host FP32 inputs: copy in pieces of piece_rows rows overlapped with
+        the first layers (0 = automatic size), or one whole copy (< 0)."""
+        self._ck(load().sdnn_set_input_streaming(self._h, int(piece_rows)))
 
     def autotune_device(self, d_ptr, rows, record_path=None):
         """Autotuner on device-resident sample rows (applies the fastest setting)."""
