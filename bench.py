@@ -574,6 +574,7 @@ CASES = {
     "chain-n4096": (4096, 60, 4096, "SNICIT", 30),
     "plain-n65536": (65536, 3, 2048, "SNIG", 3),
     "plain-n4096-30k": (4096, 3, 30000, "SNIG", 3),
+    "chain-n65536": (65536, 40, 2048, "SNICIT", 30),
 }
 
 
