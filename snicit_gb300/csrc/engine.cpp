@@ -67,11 +67,12 @@ struct GraphSlot {
 
 // Streamed ingest of host FP32 rows: at most this many copy pieces per call.
 // The automatic piece holds about 128 MB of rows (0.6 ms of copy at the
-// 211 GB/s host-to-device rate measured on GB300; 8192 rows at N = 4096),
-// and at least 2048 rows: each piece costs a few microseconds per layer.
+// 211 GB/s host-to-device rate measured on GB300), clamped to 2048 .. 16384
+// rows: each piece costs a few microseconds per layer.  Measured optimum:
+// 8192 rows at N = 4096, 16384 rows at N = 1024.
 constexpr int kMaxPieces = 16;
 constexpr int64_t kDefaultPieceBytes = 128ll << 20;
-constexpr int64_t kMinPieceRows = 2048;
+constexpr int64_t kMinPieceRows = 2048, kMaxPieceRows = 16384;
 
 struct GenSpec {
   bool on = false;
@@ -1543,7 +1544,8 @@ int infer_host(sdnn_engine* e, const float* Y0, const uint64_t* bits, int64_t ro
   const int m = bits ? 0 : streamed_prefix(e);
   const int64_t piece_rows =
       e->cfg.input_piece_rows > 0 ? e->cfg.input_piece_rows
-                                  : std::max<int64_t>(kMinPieceRows, kDefaultPieceBytes / (4 * N));
+                                  : std::clamp<int64_t>(kDefaultPieceBytes / (4 * N), kMinPieceRows,
+                                                        kMaxPieceRows);
   for (int64_t off = 0; off < rows; off += e->cfg.batch) {
     const int64_t n = std::min<int64_t>(e->cfg.batch, rows - off);
     const int P = m > 0 ? (int)std::min<int64_t>(kMaxPieces, (n + piece_rows - 1) / piece_rows) : 1;

@@ -504,14 +504,15 @@ def test_chain_with_several_centroids(N, L, T):
     _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"K chain N={N}", Y32=Y32)
 
 
-@pytest.mark.parametrize("N,L,B,mode,T,merge_start,piece", [
-    (1024, 30, 2000, "SNICIT", 20, 4, 256),    # pieces run layers 0..3, merge at 4
-    (1024, 30, 2000, "SNICIT", 3, 0, 300),     # default merge start past T: pieces run to T
-    (1024, 16, 1500, "SNIG", 16, 0, 200),      # every layer per piece
-    (4096, 20, 1200, "SNICIT", 12, 3, 250),    # binary first layer per piece
-    (65536, 3, 192, "SNIG", 3, 0, 64),         # chunked binary first layer per piece
+@pytest.mark.parametrize("N,L,B,mode,T,merge_start,piece,cap", [
+    (1024, 30, 2000, "SNICIT", 20, 4, 256, 2000),  # pieces run layers 0..3, merge at 4
+    (1024, 30, 2000, "SNICIT", 3, 0, 300, 2000),   # default merge start past T: pieces run to T
+    (1024, 16, 1500, "SNIG", 16, 0, 200, 1500),    # every layer per piece
+    (4096, 20, 1200, "SNICIT", 12, 3, 250, 1200),  # binary first layer per piece
+    (65536, 3, 192, "SNIG", 3, 0, 64, 192),        # chunked binary first layer per piece
+    (1024, 30, 2000, "SNICIT", 20, 4, 128, 700),   # three batches per call, each streamed
 ])
-def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, piece):
+def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, piece, cap):
     """Host FP32 rows copied in pieces, with the layers before the first
     cross-row step run per piece while later pieces copy, give the bits of the
     one-copy run (categories, activations, per-layer row counts), also with
@@ -522,20 +523,22 @@ def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, pie
     Y0[::7] *= 0.5  # some tiles hold other values than 0 and 1
     out = {}
     for streamed in (False, True):
-        with sg.Engine(N, L, mode=mode, threshold=T, batch=B, bias=bias, merge_start=merge_start,
+        with sg.Engine(N, L, mode=mode, threshold=T, batch=cap, bias=bias, merge_start=merge_start,
                        streamed_input=streamed, input_piece_rows=piece) as eng:
             eng.generate_weights(seed)
             flags, ids = eng.infer(Y0)
             st = eng.stats()
-            out[streamed] = (flags, ids, eng.activations(B), eng.layer_rows(), st)
+            # activations and row counts are those of the last batch of the call
+            out[streamed] = (flags, ids, eng.activations(B - (B - 1) // cap * cap),
+                             eng.layer_rows(), st)
             flags2, ids2 = eng.infer(Y0)  # graphs and buffers reused
             assert np.array_equal(flags2, flags) and np.array_equal(ids2, ids)
     assert out[False][4]["input_pieces"] == 0
-    assert out[True][4]["input_pieces"] == -(-B // piece), out[True][4]
+    assert out[True][4]["input_pieces"] == -(-min(B, cap) // piece), out[True][4]
     assert np.array_equal(out[True][1], out[False][1])
     assert np.array_equal(out[True][0], out[False][0])
     assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
     assert np.array_equal(out[True][3], out[False][3])
-    if N <= 4096:
+    if N <= 4096 and cap == B:
         Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
         _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"streamed N={N}", Y32=Y32)
