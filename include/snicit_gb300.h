@@ -99,6 +99,10 @@ typedef struct sdnn_config {
                                            /* per-layer launches where it cannot run)     */
 #define SDNN_FLAG_NO_STREAMED_INPUT 64     /* host FP32 inputs: one copy of the whole batch */
                                            /* before the first layer (no piecewise ingest) */
+#define SDNN_FLAG_HOST_POST_CHOICE 128     /* SNICIT: the host reads back what the          */
+                                           /* clustering left and picks the post-threshold  */
+                                           /* path (a host sync mid-inference) instead of   */
+                                           /* the device choosing it inside one graph       */
 
 /* Per-call statistics (stage split of SNICIT.hpp:351-354,659-664). */
 typedef struct sdnn_stats {
@@ -127,6 +131,9 @@ typedef struct sdnn_stats {
                             launch per layer, 2 cluster chain kernel (weights from
                             L2), 3 cluster chain kernel (weights streamed to shared
                             memory), 4 grid-wide chain kernel                     */
+  int32_t device_post_choice; /* SNICIT: 1 when the post-threshold path was chosen on
+                            the device (the whole inference one graph launch)     */
+  int32_t reserved1;
 } sdnn_stats;
 
 typedef struct sdnn_engine sdnn_engine;

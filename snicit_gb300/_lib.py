@@ -17,6 +17,7 @@ FLAG_NO_MERGE = 8
 FLAG_NO_CHAIN_STREAM = 16
 FLAG_NO_GRID_CHAIN = 32
 FLAG_NO_STREAMED_INPUT = 64
+FLAG_HOST_POST_CHOICE = 128
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",
@@ -55,7 +56,8 @@ class Stats(ctypes.Structure):
         ("pre_row_layers", ctypes.c_int64), ("post_row_layers", ctypes.c_int64),
         ("weight_nnz", ctypes.c_int64), ("centroid_candidates", ctypes.c_int32),
         ("merge_start", ctypes.c_int32), ("merge_every", ctypes.c_int32),
-        ("post_kernel", ctypes.c_int32),
+        ("post_kernel", ctypes.c_int32), ("device_post_choice", ctypes.c_int32),
+        ("reserved1", ctypes.c_int32),
     ]
 
 

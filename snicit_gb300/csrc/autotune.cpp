@@ -133,16 +133,19 @@ int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
     else sdnn::engine_set_snicit(e, cfg0.threshold, cfg0.num_centroids);
     if (merge_on && bs.ms < 1e30f) {
       // first layer after which identical rows are merged: early merging finds
-      // duplicates sooner, late merging skips hashing rows that are all distinct
-      // (merging after every layer, or every second one: half the hashing)
+      // duplicates sooner, late merging skips hashing rows that are all distinct;
+      // and the spacing of the later merge steps (each costs three launches)
       Trial bm = bs;
       int best_every = cfg0.merge_every;
-      for (int every : {1, 2}) {
-        for (int ms : {2, 4, 6, 8, 10}) {
+      for (int every : {1, 2, 4, 8}) {
+        for (int ms : {2, 4, 6, 8, 10, 12, 16}) {
+          if (ms >= bs.threshold) continue;  // no merge below the threshold
           sdnn::engine_set_merge(e, ms, every, true);
           Trial t{bs.tile, bs.threads, bs.threshold, bs.centroids, ms, 0.f, 0, 0};
           t.status = time_setting(e, smp, -1, t.ms, t.survivors);
-          record(f, every == 1 ? "merge" : "merge_every2", t, smp.rows);
+          char phase[24];
+          std::snprintf(phase, sizeof phase, "merge_every%d", every);
+          record(f, phase, t, smp.rows);
           if (t.status == SDNN_OK && t.ms < bm.ms) {
             bm = t;
             best_every = every;

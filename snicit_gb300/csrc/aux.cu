@@ -34,6 +34,28 @@ void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s) {
 __global__ void set_scalar_kernel(int32_t* p, int32_t v) { *p = v; }
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s) { set_scalar_kernel<<<1, 1, 0, s>>>(p, v); }
 
+__global__ void post_choice_kernel(const PostChoiceArgs a, cudaGraphConditionalHandle h) {
+  const int residues = *a.rcount, centroids = *a.ccount;
+  int body = 0;
+  if (!a.no_chain && residues == 0 && centroids >= 1) {
+    int i = 0, kc = 1;
+    while (kc < centroids) {
+      kc *= 2;
+      ++i;
+    }
+    if (i < 4) {
+      // the cluster kernel where the rows fit shared memory, else the grid kernel
+      if (centroids <= a.chain_cap && a.has_body[1 + 2 * i]) body = 1 + 2 * i;
+      else if (centroids <= a.grid_cap && a.has_body[2 + 2 * i]) body = 2 + 2 * i;
+    }
+  }
+  cudaGraphSetConditional(h, (unsigned)body);
+  *a.choice = body;
+}
+void launch_post_choice(const PostChoiceArgs& a, cudaGraphConditionalHandle h, cudaStream_t s) {
+  post_choice_kernel<<<1, 1, 0, s>>>(a, h);
+}
+
 __global__ void sum_piece_counts_kernel(const int32_t* pc, int pieces, int stride, int layers,
                                         int32_t* counts) {
   for (int l = threadIdx.x; l < layers; l += blockDim.x) {

@@ -74,6 +74,16 @@ constexpr int kMaxPieces = 16;
 constexpr int64_t kDefaultPieceBytes = 128ll << 20;
 constexpr int64_t kMinPieceRows = 2048, kMaxPieceRows = 16384;
 
+// One SNICIT inference as one graph: PH_PRE, the device-side choice of the
+// post-threshold path (a SWITCH node over kPostBodies bodies), PH_FINISH.
+struct FullGraph {
+  cudaGraphExec_t exec = nullptr;
+  GraphKey key;
+  int launches = 0;                    // PH_PRE, the choice kernel, PH_FINISH
+  int body_launches[kPostBodies] = {};
+  int variant[4] = {};                 // cluster chain variant per 2^i rows (stats)
+};
+
 struct GenSpec {
   bool on = false;
   uint64_t seed = 0;
@@ -177,6 +187,11 @@ struct sdnn_engine {
   // graph cache: one captured graph per phase of an inference (slots 5 and 6:
   // PH_ALL and PH_PRE starting after the layers run piece by piece)
   GraphSlot graphs[7];
+  FullGraph full[2];       // SNICIT whole-inference graphs (pipe_start 0 / > 0)
+  bool full_off = false;   // building one failed: the host picks the post path
+  bool in_body = false;    // capturing a conditional body (no event records)
+  int last_full = 0;       // 1 + slot of the whole-inference graph that ran last, 0: none
+  int32_t* d_choice = nullptr;  // body taken by the last whole-inference graph
   int run_launches = 0;
   int32_t* h_counts = nullptr;  // pinned: residue rows and centroids after clustering
   int chain_cap = 0;            // centroid rows the cluster chain kernel can carry
@@ -272,6 +287,7 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_mtmp);
   dfree(e->d_mcount);
   dfree(e->d_pcounts);
+  dfree(e->d_choice);
   dfree(e->d_plist[0]);
   dfree(e->d_plist[1]);
   dfree(e->d_tmask2);
@@ -287,6 +303,10 @@ void drop_graph(sdnn_engine* e) {
   for (auto& g : e->graphs) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = GraphSlot{};
+  }
+  for (auto& g : e->full) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = FullGraph{};
   }
 }
 
@@ -427,6 +447,7 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_fbcount, 16));
   T(A(&e->d_rows, 16));
   T(A(&e->d_pcounts, (size_t)kMaxPieces * (e->L + 2) * 4));
+  T(A(&e->d_choice, 16));
   T(A(&e->d_plist[0], (size_t)cap * 4));
   T(A(&e->d_plist[1], (size_t)cap * 4));
   T(A(&e->d_tmask2, (size_t)(cap + 1) * 4));
@@ -754,6 +775,7 @@ int layer_launch(sdnn_engine* e, int l, int epi, const float* in, float* out, co
 }
 
 int record(sdnn_engine* e, int i, bool capturing) {
+  if (e->in_body) return SDNN_OK;  // conditional bodies hold no event records
   if (capturing) {
     CK(cudaEventRecordWithFlags(e->ev[i], e->stream, cudaEventRecordExternal));
   } else {
@@ -1089,6 +1111,144 @@ int run_phase(sdnn_engine* e, int slot, int phase, int64_t rows, const float* d_
   return SDNN_OK;
 }
 
+// Captures one SNICIT inference into a single graph: PH_PRE, then a one-thread
+// kernel that reads what the clustering left and sets a SWITCH node's value,
+// the SWITCH node with one body per post-threshold path (the per-layer
+// launches, and the cluster / grid chain kernel for 1, 2, 4, 8 centroid rows:
+// the choices the host made after its read-back), then PH_FINISH.  No host
+// synchronisation inside an inference.  The bodies are captured after the main
+// capture has ended (each body graph belongs to the SWITCH node).
+int build_full_graph(sdnn_engine* e, FullGraph& fg, int64_t rows, const float* d_in,
+                     int32_t* d_flags) {
+  cudaGraph_t graph = nullptr;
+  CK(cudaGraphCreate(&graph, 0));
+  int rc = SDNN_OK;
+  auto give_up = [&](int code) {
+    cudaGraphDestroy(graph);
+    cudaGetLastError();
+    e->in_body = false;
+    return code;
+  };
+  cudaGraphConditionalHandle h{};
+  cudaError_t r = cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault);
+  if (r != cudaSuccess) return give_up(cuda_fail(e, r, "cudaGraphConditionalHandleCreate"));
+
+  PostChoiceArgs pc{};
+  pc.rcount = e->d_rcounts;
+  pc.ccount = e->d_ccount;
+  pc.choice = e->d_choice;
+  pc.chain_cap = e->chain_cap;
+  pc.grid_cap = grid_chain_capacity();
+  pc.no_chain = (e->cfg.flags & SDNN_FLAG_NO_CHAIN) ? 1 : 0;
+  pc.has_body[0] = 1;
+  const bool grid_ok = e->d_gscratch && !(e->cfg.flags & SDNN_FLAG_NO_GRID_CHAIN);
+  for (int i = 0; i < 4; ++i) {
+    fg.variant[i] = 0;
+    if (e->chain_cap > 0) {
+      ChainArgs ca{};
+      ca.N = e->N;
+      ca.G = e->G;
+      ca.stream = !(e->cfg.flags & SDNN_FLAG_NO_CHAIN_STREAM);
+      ca.wcap8 = e->chain_wcap8;
+      ca.wcap16 = e->chain_wcap16;
+      fg.variant[i] = chain_plan(ca, 1 << i).variant;
+    }
+    pc.has_body[1 + 2 * i] = fg.variant[i] >= 1;
+    pc.has_body[2 + 2 * i] = grid_ok && (1 << i) <= grid_chain_capacity();
+  }
+
+  r = cudaStreamBeginCaptureToGraph(e->stream, graph, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal);
+  if (r != cudaSuccess) return give_up(cuda_fail(e, r, "cudaStreamBeginCaptureToGraph"));
+  e->launches = 0;
+  rc = enqueue(e, PH_PRE, rows, d_in, d_flags, true);
+  cudaGraphNodeParams sw{};
+  if (rc == SDNN_OK) {
+    launch_post_choice(pc, h, e->stream);
+    e->launches++;
+    r = cudaGetLastError();
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (r == cudaSuccess) r = cudaStreamGetCaptureInfo(e->stream, &st, nullptr, &cg, &deps, nullptr, &nd);
+    sw.type = cudaGraphNodeTypeConditional;
+    sw.conditional.handle = h;
+    sw.conditional.type = cudaGraphCondTypeSwitch;
+    sw.conditional.size = kPostBodies;
+    cudaGraphNode_t node = nullptr;
+    if (r == cudaSuccess) r = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &sw);
+    if (r == cudaSuccess)
+      r = cudaStreamUpdateCaptureDependencies(e->stream, &node, nullptr, 1,
+                                              cudaStreamSetCaptureDependencies);
+    if (r != cudaSuccess) rc = cuda_fail(e, r, "post-threshold switch node");
+  }
+  if (rc == SDNN_OK) rc = record(e, 3, true);
+  if (rc == SDNN_OK) rc = enqueue(e, PH_FINISH, rows, d_in, d_flags, true);
+  cudaGraph_t captured = nullptr;
+  r = cudaStreamEndCapture(e->stream, &captured);
+  if (rc != SDNN_OK) return give_up(rc);
+  if (r != cudaSuccess) return give_up(cuda_fail(e, r, "cudaStreamEndCapture"));
+  fg.launches = e->launches;
+
+  for (int b = 0; b < kPostBodies; ++b) {
+    cudaGraph_t body = sw.conditional.phGraph_out[b];
+    fg.body_launches[b] = 0;
+    if (!pc.has_body[b]) {
+      cudaGraphNode_t n;
+      r = cudaGraphAddEmptyNode(&n, body, nullptr, 0);
+      if (r != cudaSuccess) return give_up(cuda_fail(e, r, "cudaGraphAddEmptyNode"));
+      continue;
+    }
+    r = cudaStreamBeginCaptureToGraph(e->stream, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (r != cudaSuccess) return give_up(cuda_fail(e, r, "cudaStreamBeginCaptureToGraph"));
+    e->in_body = true;
+    e->launches = 0;
+    int phase = PH_POST_LAYERS;
+    if (b > 0) {
+      phase = PH_POST_CHAIN;
+      e->chain_kc = 1 << ((b - 1) / 2);
+      e->chain_kind = (b & 1) ? 1 : 2;
+    }
+    rc = enqueue(e, phase, rows, d_in, d_flags, true);
+    e->in_body = false;
+    cudaGraph_t got = nullptr;
+    r = cudaStreamEndCapture(e->stream, &got);
+    if (rc != SDNN_OK) return give_up(rc);
+    if (r != cudaSuccess) return give_up(cuda_fail(e, r, "cudaStreamEndCapture"));
+    fg.body_launches[b] = e->launches;
+  }
+  r = cudaGraphInstantiate(&fg.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (r != cudaSuccess) {
+    fg.exec = nullptr;
+    cudaGetLastError();
+    return cuda_fail(e, r, "cudaGraphInstantiate");
+  }
+  return SDNN_OK;
+}
+
+// Runs a SNICIT inference as one graph launch (built on first use).  Returns
+// SDNN_ERR_UNSUPPORTED when the graph cannot be built (the caller then lets
+// the host choose the post-threshold path, for this and every later call).
+int run_full(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
+  const int slot = e->pipe_start > 0 ? 1 : 0;
+  FullGraph& fg = e->full[slot];
+  const GraphKey key{0, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
+                     e->key.T, e->threads, 0, e->pipe_start};
+  if (!fg.exec || !(fg.key == key)) {
+    if (fg.exec) cudaGraphExecDestroy(fg.exec);
+    fg = FullGraph{};
+    if (build_full_graph(e, fg, rows, d_in, d_flags) != SDNN_OK) return SDNN_ERR_UNSUPPORTED;
+    fg.key = key;
+  }
+  CK(cudaGraphLaunch(fg.exec, e->stream));
+  e->run_launches += fg.launches;
+  e->last_full = 1 + slot;
+  return SDNN_OK;
+}
+
 int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   if (rows <= 0) return fail(e, SDNN_ERR_INVALID, "rows must be positive");
   if (rows > e->cap) return fail(e, SDNN_ERR_INVALID, "rows exceed the batch capacity");
@@ -1101,7 +1261,22 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   launch_set_scalar(e->d_rows, (int32_t)rows, e->stream);
   e->run_launches++;
   int rc;
-  if (e->cfg.mode != SDNN_MODE_SNICIT || T >= e->L) {
+  e->last_full = 0;
+  const bool full = e->cfg.mode == SDNN_MODE_SNICIT && T < e->L && !e->full_off &&
+                    !(e->cfg.flags & SDNN_FLAG_HOST_POST_CHOICE);
+  if (full) {
+    rc = run_full(e, rows, d_in, d_flags);
+    if (rc == SDNN_ERR_UNSUPPORTED) {
+      // the graph could not be built here: the host chooses from now on
+      e->full_off = true;
+      e->err.clear();
+    } else if (rc) {
+      return rc;
+    }
+  }
+  if (e->last_full) {
+    // post-threshold path chosen on the device (stats read it back later)
+  } else if (e->cfg.mode != SDNN_MODE_SNICIT || T >= e->L) {
     e->last_post_kernel = 0;
     if ((rc = run_phase(e, 0, PH_ALL, rows, d_in, d_flags))) return rc;
   } else {
@@ -1235,6 +1410,16 @@ int collect_stats(sdnn_engine* e) {
   st.merge_start = merging_on(e) ? (e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart) : 0;
   st.merge_every = merging_on(e) ? std::max(1, e->cfg.merge_every) : 0;
   st.post_kernel = e->last_post_kernel;
+  if (e->last_full) {
+    // the device chose the post-threshold path: which body ran
+    const FullGraph& fg = e->full[e->last_full - 1];
+    int32_t b = 0;
+    CK(cudaMemcpy(&b, e->d_choice, 4, cudaMemcpyDeviceToHost));
+    if (b < 0 || b >= kPostBodies) b = 0;
+    st.post_kernel = b == 0 ? 1 : (b & 1) ? 1 + fg.variant[(b - 1) / 2] : 4;
+    st.launches += fg.body_launches[b];
+    st.device_post_choice = 1;
+  }
   e->pending_stats = 0;
   return SDNN_OK;
 }

@@ -163,6 +163,22 @@ cudaError_t launch_grid_chain(const GridChainArgs& a, int kc_needed, int num_sms
 // ---- auxiliary kernels (aux.cu) ----
 void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s);
+
+// Post-threshold path chosen on the device, inside the inference's graph: a
+// one-thread kernel reads what the clustering left and sets the value of the
+// graph's SWITCH node -- body 0 the per-layer centroid/residue launches, body
+// 1 + 2i the cluster chain kernel and body 2 + 2i the grid chain kernel for
+// 2^i centroid rows (i < 4); bodies the engine could not build are absent
+// (has_body 0) and never chosen.  The choice is also stored for the stats.
+constexpr int kPostBodies = 9;
+struct PostChoiceArgs {
+  const int32_t* rcount;  // residue rows at the threshold
+  const int32_t* ccount;  // centroids kept
+  int32_t* choice;        // out: the body taken
+  int32_t chain_cap, grid_cap, no_chain;
+  int32_t has_body[kPostBodies];
+};
+void launch_post_choice(const PostChoiceArgs& a, cudaGraphConditionalHandle h, cudaStream_t s);
 // counts[l] = sum over pieces p of piece_counts[p * stride + l], l < layers
 // (row counts of the layers run piece by piece).
 void launch_sum_piece_counts(const int32_t* piece_counts, int pieces, int stride, int layers,

@@ -314,7 +314,8 @@ def test_chain_path_is_bitwise_equal_to_per_layer_path(N, L, B, T, K):
     Y0 = sg.generate_inputs(N, seed, 0, B)
     runs = {"layers": dict(chain=False), "default": dict(),
             "cluster_l2": dict(chain_stream=False, grid_chain=False),
-            "grid": dict(chain_stream=False, chain=True)}
+            "grid": dict(chain_stream=False, chain=True),
+            "host_choice": dict(device_post_choice=False)}
     out = {}
     for name, kw in runs.items():
         with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=B, bias=bias, num_centroids=K,
@@ -324,10 +325,16 @@ def test_chain_path_is_bitwise_equal_to_per_layer_path(N, L, B, T, K):
             out[name] = (flags, ids, eng.activations(B), eng.stats(), eng.layer_rows())
     kinds = {k: v[3]["post_kernel"] for k, v in out.items()}
     assert kinds["layers"] == 1
+    # the device picks the post-threshold path inside one graph, as the host would
+    assert out["default"][3]["device_post_choice"] == 1
+    assert out["host_choice"][3]["device_post_choice"] == 0
+    assert kinds["host_choice"] == kinds["default"], kinds
+    # (the device path adds the one-thread choice kernel)
+    assert out["default"][3]["launches"] == out["host_choice"][3]["launches"] + 1
     if out["layers"][3]["residue_rows"] == 0 and out["layers"][3]["centroids"] > 0:
         assert kinds["grid"] in (2, 3, 4), kinds  # a chain kernel of some kind
         assert kinds["cluster_l2"] in (1, 2), kinds
-    for k in ("default", "cluster_l2", "grid"):
+    for k in ("default", "cluster_l2", "grid", "host_choice"):
         assert np.array_equal(out[k][1], out["layers"][1])
         assert np.array_equal(out[k][2].view(np.uint32), out["layers"][2].view(np.uint32)), (k, kinds)
         assert np.array_equal(out[k][4], out["layers"][4])
