@@ -79,7 +79,7 @@ typedef struct sdnn_config {
                             are merged (0 = automatic)                            */
   int32_t merge_every;   /* ... and then after every merge_every-th layer (0 = 1)  */
   int32_t input_piece_rows; /* host FP32 inputs: rows per copy piece of the streamed
-                            ingest (0 = automatic: about 128 MB, 2048..16384 rows) */
+                            ingest (0 = automatic: about 96 MB, 2048..16384 rows)  */
   int32_t reserved[1];
 } sdnn_config;
 

@@ -66,12 +66,12 @@ struct GraphSlot {
 };
 
 // Streamed ingest of host FP32 rows: at most this many copy pieces per call.
-// The automatic piece holds about 128 MB of rows (0.6 ms of copy at the
+// The automatic piece holds about 96 MB of rows (0.45 ms of copy at the
 // 211 GB/s host-to-device rate measured on GB300), clamped to 2048 .. 16384
 // rows: each piece costs a few microseconds per layer.  Measured optimum:
-// 8192 rows at N = 4096, 16384 rows at N = 1024.
+// about 6000 rows at N = 4096, 16384 rows at N = 1024.
 constexpr int kMaxPieces = 16;
-constexpr int64_t kDefaultPieceBytes = 128ll << 20;
+constexpr int64_t kDefaultPieceBytes = 96ll << 20;
 constexpr int64_t kMinPieceRows = 2048, kMaxPieceRows = 16384;
 
 // One SNICIT inference as one graph: PH_PRE, the device-side choice of the
@@ -1656,9 +1656,12 @@ int run_streamed(sdnn_engine* e, const float* Y0, int64_t n, int m, int P) {
   // the copies overwrite d_in: only after everything enqueued so far
   CK(cudaEventRecord(e->ingest_free, s));
   CK(cudaStreamWaitEvent(e->copy_stream, e->ingest_free, 0));
+  // piece boundaries on 32-row tiles; the last piece is half as large as the
+  // others: its layers are the ingest work left once the final copy has landed
   int64_t bnd[kMaxPieces + 1];
-  for (int p = 0; p <= P; ++p)  // piece boundaries on 32-row tiles
-    bnd[p] = p == P ? n : std::min<int64_t>(n, (n * p / P + 31) / 32 * 32);
+  const double span = P - 0.5;
+  for (int p = 0; p <= P; ++p)
+    bnd[p] = p == P ? n : std::min<int64_t>(n, ((int64_t)((double)n * p / span) + 31) / 32 * 32);
   for (int p = 0; p < P; ++p) {
     const int64_t rows = bnd[p + 1] - bnd[p];
     if (rows > 0)
