@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SDNN_ABI_VERSION 1
+#define SDNN_ABI_VERSION 2
 
 /* Status codes returned by every entry point. */
 typedef enum sdnn_status {
@@ -155,6 +155,11 @@ int sdnn_destroy(sdnn_engine* e);
 const char* sdnn_last_error(const sdnn_engine* e);
 const char* sdnn_status_string(int status);
 int sdnn_abi_version(void);
+/* sizeof of the public structs, for a binding to check its own layouts:
+ * out[0..3] = sdnn_config, sdnn_stats, sdnn_server_config, sdnn_server_stats
+ * (at most n entries written).  No CUDA call.  (No counterpart in the
+ * reference: its classes are used from C++ directly.) */
+int sdnn_abi_sizes(int32_t* out, int32_t n);
 
 /* ---- weights ------------------------------------------------------------ */
 

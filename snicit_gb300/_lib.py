@@ -89,6 +89,7 @@ SIGNATURES = [
     ("sdnn_last_error", ctypes.c_char_p, [P]),
     ("sdnn_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("sdnn_abi_version", ctypes.c_int, []),
+    ("sdnn_abi_sizes", ctypes.c_int, [P, I32]),
     ("sdnn_load_weights_tsv", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_set_layer_coo", ctypes.c_int, [P, I32, P, P, P, I64]),
     ("sdnn_set_layer_bias", ctypes.c_int, [P, I32, P]),

@@ -1432,6 +1432,14 @@ extern "C" {
 
 int sdnn_abi_version(void) { return SDNN_ABI_VERSION; }
 
+int sdnn_abi_sizes(int32_t* out, int32_t n) {
+  if (!out || n < 0) return SDNN_ERR_INVALID;
+  const int32_t sizes[4] = {(int32_t)sizeof(sdnn_config), (int32_t)sizeof(sdnn_stats),
+                            (int32_t)sizeof(sdnn_server_config), (int32_t)sizeof(sdnn_server_stats)};
+  for (int32_t i = 0; i < n && i < 4; ++i) out[i] = sizes[i];
+  return SDNN_OK;
+}
+
 const char* sdnn_status_string(int status) {
   switch (status) {
     case SDNN_OK: return "ok";

@@ -43,7 +43,17 @@ def test_defaults_and_reference_bias():
     # main/SDGC.cu:49-54
     for n, b in ((65536, -0.45), (16384, -0.4), (4096, -0.35), (1024, -0.3), (77, 0.0)):
         assert lib.sdnn_reference_bias(n) == pytest.approx(b)
-    assert lib.sdnn_abi_version() == 1
+    assert lib.sdnn_abi_version() == 2
+
+
+def test_struct_layouts_match_the_c_abi():
+    """The ctypes mirrors of the public structs have the C sizes (a field
+    added on one side only would shift every later field)."""
+    lib = _lib.load()
+    sizes = (ctypes.c_int32 * 4)()
+    assert lib.sdnn_abi_sizes(sizes, 4) == 0
+    want = [ctypes.sizeof(c) for c in (_lib.Config, _lib.Stats, _lib.ServerConfig, _lib.ServerStats)]
+    assert list(sizes) == want
     assert lib.sdnn_status_string(7) == b"device wait timed out"
 
 
