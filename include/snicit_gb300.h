@@ -80,7 +80,10 @@ typedef struct sdnn_config {
   int32_t merge_every;   /* ... and then after every merge_every-th layer (0 = 1)  */
   int32_t input_piece_rows; /* host FP32 inputs: rows per copy piece of the streamed
                             ingest (0 = automatic: about 96 MB, 2048..16384 rows)  */
-  int32_t reserved[1];
+  int32_t input_prefix_layers; /* streamed ingest, SNICIT with merging: the pieces
+                            run the layers up to the latest scheduled merge layer
+                            <= this (their merges deferred to it; exact, same bits);
+                            0 = up to the first merge layer                      */
 } sdnn_config;
 
 /* sdnn_config.flags: switch off layout optimisations (results are identical

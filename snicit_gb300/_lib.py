@@ -41,7 +41,7 @@ class Config(ctypes.Structure):
         ("tile_rows", ctypes.c_int32), ("threads", ctypes.c_int32),
         ("flags", ctypes.c_int32), ("merge_start", ctypes.c_int32),
         ("merge_every", ctypes.c_int32), ("input_piece_rows", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 1),
+        ("input_prefix_layers", ctypes.c_int32),
     ]
 
 

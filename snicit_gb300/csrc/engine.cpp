@@ -1621,9 +1621,15 @@ int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows, int32_t* 
   return rc;
 }
 
-// First layer of the cross-row part of an inference (the first merge step in
-// SNICIT mode, else the threshold clustering; L in SNIG mode): the layers
-// before it may run piece by piece.  0 when host inputs are not streamed.
+// First layer of the cross-row part of an inference (a merge step in SNICIT
+// mode, else the threshold clustering; L in SNIG mode): the layers before it
+// may run piece by piece.  0 when host inputs are not streamed.
+//
+// With merging the pieces may run past the first merge layer up to a later
+// scheduled one, k: the merges before k are skipped and the one after layer
+// k - 1 merges everything they would have merged (rows that are equal stay
+// equal, and every set of equal rows keeps its smallest row id either way), so
+// from layer k on the rows, and all results, are the same bits.
 int streamed_prefix(const sdnn_engine* e) {
   if (e->cfg.flags & SDNN_FLAG_NO_STREAMED_INPUT) return 0;
   if (e->cfg.mode != SDNN_MODE_SNIG && e->cfg.mode != SDNN_MODE_SNICIT) return 0;
@@ -1631,7 +1637,11 @@ int streamed_prefix(const sdnn_engine* e) {
   int m = T;
   if (merging_on(e)) {
     const int start = e->cfg.merge_start > 0 ? e->cfg.merge_start : kMergeStart;
-    if (start < T) m = std::min(m, start);
+    const int every = e->cfg.merge_every > 0 ? e->cfg.merge_every : 1;
+    if (start < T) {
+      m = start;
+      while (m + every < T && m + every <= e->cfg.input_prefix_layers) m += every;
+    }
   }
   return m;
 }

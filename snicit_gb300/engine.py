@@ -24,7 +24,7 @@ class Engine:
                  device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
                  chain=True, merge=True, merge_start=0, merge_every=0, chain_stream=True,
                  grid_chain=True, streamed_input=True, input_piece_rows=0,
-                 device_post_choice=True):
+                 device_post_choice=True, input_prefix_layers=0):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -51,6 +51,7 @@ class Engine:
         cfg.merge_start = int(merge_start)
         cfg.merge_every = int(merge_every)
         cfg.input_piece_rows = int(input_piece_rows)
+        cfg.input_prefix_layers = int(input_prefix_layers)
         self.cfg = cfg
         self.N = cfg.num_neurons
         self.L = cfg.num_layers

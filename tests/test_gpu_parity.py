@@ -511,15 +511,17 @@ def test_chain_with_several_centroids(N, L, T):
     _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"K chain N={N}", Y32=Y32)
 
 
-@pytest.mark.parametrize("N,L,B,mode,T,merge_start,piece,cap", [
-    (1024, 30, 2000, "SNICIT", 20, 4, 256, 2000),  # pieces run layers 0..3, merge at 4
-    (1024, 30, 2000, "SNICIT", 3, 0, 300, 2000),   # default merge start past T: pieces run to T
-    (1024, 16, 1500, "SNIG", 16, 0, 200, 1500),    # every layer per piece
-    (4096, 20, 1200, "SNICIT", 12, 3, 250, 1200),  # binary first layer per piece
-    (65536, 3, 192, "SNIG", 3, 0, 64, 192),        # chunked binary first layer per piece
-    (1024, 30, 2000, "SNICIT", 20, 4, 128, 700),   # three batches per call, each streamed
+@pytest.mark.parametrize("N,L,B,mode,T,merge_start,piece,cap,prefix", [
+    (1024, 30, 2000, "SNICIT", 20, 4, 256, 2000, 0),   # pieces run layers 0..3, merge at 4
+    (1024, 30, 2000, "SNICIT", 3, 0, 300, 2000, 0),    # default merge start past T: to T
+    (1024, 16, 1500, "SNIG", 16, 0, 200, 1500, 0),     # every layer per piece
+    (4096, 20, 1200, "SNICIT", 12, 3, 250, 1200, 0),   # binary first layer per piece
+    (65536, 3, 192, "SNIG", 3, 0, 64, 192, 0),         # chunked binary first layer per piece
+    (1024, 30, 2000, "SNICIT", 20, 4, 128, 700, 0),    # three batches per call, each streamed
+    (1024, 30, 2000, "SNICIT", 20, 4, 256, 2000, 12),  # merges 4..11 deferred to layer 12
+    (4096, 40, 1500, "SNICIT", 30, 6, 300, 1500, 40),  # deferred to the last merge layer (29)
 ])
-def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, piece, cap):
+def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, piece, cap, prefix):
     """Host FP32 rows copied in pieces, with the layers before the first
     cross-row step run per piece while later pieces copy, give the bits of the
     one-copy run (categories, activations, per-layer row counts), also with
@@ -531,7 +533,8 @@ def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, pie
     out = {}
     for streamed in (False, True):
         with sg.Engine(N, L, mode=mode, threshold=T, batch=cap, bias=bias, merge_start=merge_start,
-                       streamed_input=streamed, input_piece_rows=piece) as eng:
+                       streamed_input=streamed, input_piece_rows=piece,
+                       input_prefix_layers=prefix) as eng:
             eng.generate_weights(seed)
             flags, ids = eng.infer(Y0)
             st = eng.stats()
@@ -545,7 +548,17 @@ def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, pie
     assert np.array_equal(out[True][1], out[False][1])
     assert np.array_equal(out[True][0], out[False][0])
     assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
-    assert np.array_equal(out[True][3], out[False][3])
+    rows_t, rows_f = out[True][3], out[False][3]
+    if prefix:
+        # deferred merges: more rows in the layers between the first merge layer
+        # and the one the pieces ran to, the same counts before and after
+        m = merge_start
+        while m + 1 < T and m + 1 <= prefix:
+            m += 1
+        assert np.all(rows_t[merge_start:m] >= rows_f[merge_start:m])
+        rows_t = np.concatenate([rows_t[:merge_start], rows_t[m:]])
+        rows_f = np.concatenate([rows_f[:merge_start], rows_f[m:]])
+    assert np.array_equal(rows_t, rows_f)
     if N <= 4096 and cap == B:
         Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
         _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"streamed N={N}", Y32=Y32)
