@@ -562,3 +562,50 @@ def test_streamed_host_input_is_bitwise_equal(N, L, B, mode, T, merge_start, pie
     if N <= 4096 and cap == B:
         Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
         _check(out[True][2], out[True][0], out[True][1], Yref, alive, f"streamed N={N}", Y32=Y32)
+
+
+@pytest.mark.parametrize("N,L", [(4096, 480), (16384, 1920)])
+def test_full_size_workload_snicit_equals_plain(N, L):
+    """The SDGC-shaped workloads at full size (60000 seeded binary rows, 32
+    nonzeros of 0.0625 per row, the reference bias): SNICIT (merging, the
+    threshold at 30, chain kernels) gives the plain per-layer path's category
+    set exactly, twice over (bitwise repeatable), and -- at N = 4096 -- the
+    streamed host ingest gives the device path's flags and the first 32 rows
+    match the FP64 oracle."""
+    torch = pytest.importorskip("torch")
+    B, seed = 60000, 20260101
+    bias = sg.load().sdnn_reference_bias(N)
+    d_in = torch.empty((B, N), dtype=torch.float32, device="cuda")
+    sg.generate_inputs_device(N, seed, 0, B, d_in.data_ptr())
+    d_flags = torch.zeros(B, dtype=torch.int32, device="cuda")
+    with sg.Engine(N, L, mode="SNICIT", threshold=30, batch=B, bias=bias, num_centroids=50,
+                   merge_start=10, merge_every=2) as eng:
+        eng.generate_weights(seed, 32, 0.0625)
+        runs = []
+        for _ in range(2):
+            d_flags.zero_()
+            eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr())
+            torch.cuda.synchronize()
+            runs.append(d_flags.cpu().numpy().copy())
+        st = eng.stats()
+        assert st["device_post_choice"] == 1
+        assert np.array_equal(runs[0], runs[1])
+        snicit = runs[0]
+        assert 0.01 * B < snicit.sum() < 0.99 * B
+        if N == 4096:
+            host = d_in.cpu().numpy()
+            flags_h, ids_h = eng.infer(host)
+            assert eng.stats()["input_pieces"] > 1
+            assert np.array_equal(flags_h, snicit)
+            assert np.array_equal(ids_h, np.flatnonzero(snicit))
+            del host
+        eng.set_mode("SNIG", L)
+        d_flags.zero_()
+        eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr())
+        torch.cuda.synchronize()
+        plain = d_flags.cpu().numpy().copy()
+    assert np.array_equal(snicit, plain)
+    if N == 4096:
+        Y0 = sg.generate_inputs(N, seed, 0, 32)
+        _, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64, want_y=False)
+        assert np.array_equal(snicit[:32], alive.astype(np.int32))
