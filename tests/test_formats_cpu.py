@@ -100,3 +100,83 @@ def test_pack_bits_matches_the_file_encoding(tmp_path):
     sg.write_inputs_bin(path, Y, bits=True)
     words = np.frombuffer(path.read_bytes()[32:], dtype=np.uint64).reshape(11, -1)
     assert np.array_equal(sg.pack_bits(Y), words)
+
+
+def _read_packed(path):
+    """Parses a packed-weight file (layout in csrc/packfile.h) into numpy
+    arrays, one dict per layer."""
+    b = path.read_bytes()
+    magic = b[:8]
+    N, L, Q, nq, G, placed, scale = np.frombuffer(b, np.int32, 7, 8)
+    assert magic == b"SDNNPK01"
+    pad = lambda n: (n + 63) // 64 * 64
+    off, layers = 64, []
+    for _ in range(L):
+        constw, = np.frombuffer(b, np.int32, 1, off)
+        nnz, nblocks, slots = np.frombuffer(b, np.int64, 3, off + 8)
+        has_bias, = np.frombuffer(b, np.int32, 1, off + 40)
+        off += 64
+        grp = np.frombuffer(b, np.int32, G * nq + 1, off)
+        off += pad((G * nq + 1) * 4)
+        idx = np.frombuffer(b, np.uint16, nblocks * 128, off).reshape(nblocks, 32, 4)
+        off += pad(nblocks * 128 * 2)
+        if not constw:
+            off += pad(nblocks * 128 * 4)
+        if has_bias:
+            off += pad(N * 4)
+        pos = None
+        if placed:
+            pos = np.frombuffer(b, np.int32, N, off)
+            off += pad(N * 4)
+        layers.append(dict(grp=grp, idx=idx, pos=pos, nnz=int(nnz)))
+    return dict(N=int(N), Q=int(Q), nq=int(nq), G=int(G), scale=int(scale), layers=layers)
+
+
+@pytest.mark.parametrize("N,L,placement", [(256, 2, False), (1024, 3, True), (4096, 2, True),
+                                           (16384, 2, True), (65536, 1, True)])
+def test_packed_layout_is_bank_conflict_free_and_holds_every_edge(tmp_path, N, L, placement):
+    """The layout every layer kernel relies on: in each slot the 32 lanes'
+    indices (edges and padding alike) fall in 32 distinct shared-memory banks;
+    the real slots hold exactly the layer's edges (input position -> output
+    position, mapped back to neurons through the placement); and a (group,
+    chunk) takes exactly the lower bound max(largest lane degree, largest bank
+    degree) of slots, rounded up to a block of 4."""
+    seed, path = 11, tmp_path / "w.sdnnw"
+    with sg.Engine(N, L, mode="SNICIT", batch=8, placement=placement) as e:
+        e.generate_weights(seed)
+        e.save_packed(path)
+    f = _read_packed(path)
+    Q, nq, G, scale = f["Q"], f["nq"], f["G"], f["scale"]
+    prev_inv = np.arange(N)  # input position -> neuron (layer 0: the caller's order)
+    for l, lay in enumerate(f["layers"]):
+        idx, grp = lay["idx"], lay["grp"]
+        jl = idx.astype(np.int64) // scale  # chunk-local index per (block, lane, slot)
+        banks = jl % 32
+        # distinct banks per slot: sort the 32 lanes' banks of every (block, slot)
+        per_slot = np.sort(banks.transpose(0, 2, 1), axis=2)
+        assert np.array_equal(per_slot, np.broadcast_to(np.arange(32), per_slot.shape))
+        real = jl < Q
+        inv = np.argsort(lay["pos"]) if lay["pos"] is not None else np.arange(N)
+        got_in, got_out = [], []
+        for g in range(G):
+            for q in range(nq):
+                b0, b1 = grp[g * nq + q], grp[g * nq + q + 1]
+                if b1 == b0:
+                    continue
+                m = real[b0:b1]                      # [blocks, lane, slot]
+                lanes = np.broadcast_to(np.arange(32)[None, :, None], m.shape)
+                got_in.append(q * Q + jl[b0:b1][m])
+                got_out.append(32 * g + lanes[m])
+                # slot count against the lower bound of this (group, chunk)
+                lane_deg = m.sum(axis=(0, 2))
+                bank_deg = np.bincount(banks[b0:b1][m], minlength=32)
+                bound = max(lane_deg.max(), bank_deg.max())
+                # (an edge colouring with exactly that many colours, blocks of 4)
+                assert 4 * (b1 - b0) == (bound + 3) // 4 * 4, (l, g, q, b1 - b0, bound)
+        got_in = prev_inv[np.concatenate(got_in)]
+        got_out = inv[np.concatenate(got_out)]
+        r, c, _ = sg.generate_layer_coo(N, seed, l, 32, 0.0625)
+        assert len(got_in) == len(r) == lay["nnz"]
+        want = np.sort(r.astype(np.int64) * N + c)
+        assert np.array_equal(np.sort(got_in * N + got_out), want)
+        prev_inv = inv
