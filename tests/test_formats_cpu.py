@@ -179,4 +179,7 @@ def test_packed_layout_is_bank_conflict_free_and_holds_every_edge(tmp_path, N, L
         assert len(got_in) == len(r) == lay["nnz"]
         want = np.sort(r.astype(np.int64) * N + c)
         assert np.array_equal(np.sort(got_in * N + got_out), want)
+        if placement and l >= 1 and nq == 1:
+            # the placement balances this layer's banks (measured 0.86-0.87)
+            assert lay["nnz"] / (idx.shape[0] * 128) >= 0.8
         prev_inv = inv
