@@ -7,7 +7,7 @@ and weights with numpy, runs oracle/ref_harness.cpp, and stores inputs,
 weights and the reference kernels' final activations and categories as
 <case>.npz.  The CPU tests then check the oracle against these files.
 
-    python tests/golden/make_golden.py OUT_DIR
+    python tests/golden/make_golden.py [OUT_DIR]      (default: tests/golden/)
 """
 import os
 import struct
@@ -96,4 +96,4 @@ def main(out_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__)))
