@@ -113,18 +113,21 @@ def make_layers_csr(sg, N, L):
     return [sg.generate_layer_csr(N, SEED, l, NNZ, 0.0625) for l in range(L)]
 
 
-def cpu_port_rate(sg, N, L, bias, rows_budget_s=12.0, offset=0, layers=None):
-    """FP32 oracle port on a bounded sample; returns (edges/s, rows, seconds, threads)."""
+def cpu_port_rate(sg, N, L, bias, rows_budget_s=12.0, offset=0, layers=None, row_s=None):
+    """FP32 oracle port on a bounded sample; returns (edges/s, rows, seconds,
+    threads, layers).  row_s: seconds per row from an earlier sample (else a
+    probe of a few rows measures it)."""
     from oracle import oracle as orc
     if layers is None:
         layers = make_layers_csr(sg, N, L)
     threads = os.cpu_count() or 1
     probe = max(threads, 32)
-    Y = sg.generate_inputs(N, SEED, offset, probe)
-    t0 = time.perf_counter()
-    orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
-    dt = time.perf_counter() - t0
-    rows = int(min(20000, max(probe, probe * rows_budget_s / max(dt, 1e-3))))
+    if row_s is None:
+        Y = sg.generate_inputs(N, SEED, offset, probe)
+        t0 = time.perf_counter()
+        orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
+        row_s = max(time.perf_counter() - t0, 1e-3) / probe
+    rows = int(min(20000, max(probe, rows_budget_s / row_s)))
     Y = sg.generate_inputs(N, SEED, offset, rows)
     t0 = time.perf_counter()
     orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
@@ -147,10 +150,16 @@ def run_reference(args):
     layers = make_layers_csr(sg, N, L)
     rates = []
     rows = secs = threads = 0
+    # bounded samples: about 2.5 minutes of CPU work over the timed steps and
+    # 12 s over the warm-up ones, whatever K and W are (at most 12 s a step)
+    timed = min(12.0, max(1.0, 150.0 / max(1, args.steps)))
+    warm = min(4.0, max(0.5, 12.0 / max(1, args.warmup)))
+    row_s = None  # measured once, by the first step's probe
     for step in range(args.warmup + args.steps):
-        budget = 4.0 if step < args.warmup else 12.0
+        budget = warm if step < args.warmup else timed
         r, rows, secs, threads, _ = cpu_port_rate(sg, N, L, bias, budget, offset=step * 997,
-                                                  layers=layers)
+                                                  layers=layers, row_s=row_s)
+        row_s = secs / rows
         if step >= args.warmup:
             rates.append(r)
     value = statistics.median(rates)
