@@ -21,14 +21,6 @@ static int grid_for(long work, int per_block, int cap = 4096) {
 
 // ---------------------------------------------------------------- row lists
 
-__global__ void iota_kernel(int32_t* list, int32_t* count, int32_t n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) list[i] = i;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
-}
-void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s) {
-  iota_kernel<<<grid_for(n, 256), 256, 0, s>>>(list, count, n);
-}
-
 // Rows of the current inference come from a device scalar (set just before a
 // captured graph is launched), so one graph serves every row count.
 __global__ void set_scalar_kernel(int32_t* p, int32_t v) { *p = v; }

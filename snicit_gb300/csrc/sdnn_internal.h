@@ -161,7 +161,6 @@ size_t grid_chain_scratch_floats(int layers, int nq, int Q);
 cudaError_t launch_grid_chain(const GridChainArgs& a, int kc_needed, int num_sms, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
-void launch_iota(int32_t* list, int32_t* count, int32_t n, cudaStream_t s);
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s);
 
 // Post-threshold path chosen on the device, inside the inference's graph: a
