@@ -9,7 +9,8 @@ the bound is 4x the error of a plain sequential FP32 evaluation of the same
 row (the oracle's FP32 port), i.e. per row
     tol_r = max(1e-5, 4 * err_fp32port_r).
 On long nets (the benchmark configurations) rows saturate and the bound is
-1e-5 everywhere.
+1e-5 everywhere.  The plain path is also checked bit for bit against a CPU
+evaluation in the kernels' own summation order (tests/packed_layout.py).
 """
 import os
 import tempfile
@@ -609,3 +610,33 @@ def test_full_size_workload_snicit_equals_plain(N, L):
         Y0 = sg.generate_inputs(N, seed, 0, 32)
         _, alive, _ = orc.infer(_layers(N, L, seed), N, bias, Y0, precision=64, want_y=False)
         assert np.array_equal(snicit[:32], alive.astype(np.int32))
+
+
+@pytest.mark.parametrize("N,L,B,mode,flags", [
+    (1024, 24, 300, "SNIG", {}),
+    (1024, 24, 300, "BF", {"binary_first_layer": False}),
+    (4096, 12, 200, "SNIG", {"placement": False}),
+    (16384, 6, 64, "SNIG", {}),
+    (65536, 3, 32, "SNIG", {}),
+])
+def test_plain_path_is_bitwise_equal_to_slot_order_evaluation(tmp_path, N, L, B, mode, flags):
+    """Bit-exact parity of the plain path: the kernels' activations equal, bit
+    for bit, a numpy evaluation of the recurrence in the kernels' summation
+    order read from the packed-weight file (exact products with w = 1/16, so
+    each fused multiply-add rounds like a float32 add); that evaluation agrees
+    with the FP64 oracle within the FP32 bound (checked on the CPU)."""
+    import packed_layout as pl
+    seed = 900 + N
+    bias = sg.load().sdnn_reference_bias(N)
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    path = tmp_path / "w.sdnnw"
+    with sg.Engine(N, L, mode=mode, batch=B, bias=bias, **flags) as eng:
+        eng.generate_weights(seed)
+        eng.save_packed(path)
+        got_flags, _ = eng.infer(Y0)
+        Y = eng.activations(B)
+    want = pl.plain_in_slot_order(pl.read_packed(path), Y0, bias)
+    alive = (want > 0).any(axis=1)
+    assert np.array_equal(got_flags, alive.astype(np.int32))
+    assert alive.sum() > 0
+    assert np.array_equal(Y[alive].view(np.uint32), want[alive].view(np.uint32))
