@@ -109,36 +109,43 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_layers_csr(sg, N, L):
-    return [sg.generate_layer_csr(N, SEED, l, NNZ, 0.0625) for l in range(L)]
-
-
-def cpu_port_rate(sg, N, L, bias, rows_budget_s=12.0, offset=0, layers=None, row_s=None):
-    """FP32 oracle port on a bounded sample; returns (edges/s, rows, seconds,
-    threads, layers).  row_s: seconds per row from an earlier sample (else a
-    probe of a few rows measures it)."""
+def cpu_port(N, L, bias, group_rows, row_offset=0):
+    """The oracle's FP32 restatement of bf_inference on the host cores over
+    consecutive groups of the workload's rows (the weights generated layer by
+    layer, untimed); returns (seconds per group, survivors per group, threads)."""
+    import numpy as np
     from oracle import oracle as orc
-    if layers is None:
-        layers = make_layers_csr(sg, N, L)
     threads = os.cpu_count() or 1
-    probe = max(threads, 32)
-    if row_s is None:
-        Y = sg.generate_inputs(N, SEED, offset, probe)
-        t0 = time.perf_counter()
-        orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
-        row_s = max(time.perf_counter() - t0, 1e-3) / probe
-    rows = int(min(20000, max(probe, rows_budget_s / row_s)))
-    Y = sg.generate_inputs(N, SEED, offset, rows)
-    t0 = time.perf_counter()
-    orc.infer(layers, N, bias, Y, precision=32, nthreads=threads, want_y=False)
-    dt = time.perf_counter() - t0
-    return rows * NNZ * N * L / dt, rows, dt, threads, layers
+    total = int(sum(group_rows))
+    Y = orc.gen_inputs(N, SEED, row_offset, total)
+    alive, secs, _ = orc.port_stream(N, L, SEED, bias, Y, group_rows, nnz=NNZ, value=0.0625,
+                                     nthreads=threads)
+    off = np.concatenate([[0], np.cumsum(group_rows)]).astype(np.int64)
+    surv = [int(alive[off[i]:off[i + 1]].sum()) for i in range(len(group_rows))]
+    return secs, surv, threads
+
+
+def cpu_row_seconds(N, L, bias, probe=None):
+    """Seconds of host work per input row of the workload, from a probe of a
+    few rows (all layers)."""
+    threads = os.cpu_count() or 1
+    probe = probe or max(2 * threads, 48)
+    secs, _, _ = cpu_port(N, L, bias, [probe])
+    return max(float(secs[0]), 1e-3) / probe
+
+
+def cpu_port_rate(N, L, bias, budget_s=12.0):
+    """FP32 port on a bounded sample (about budget_s of host work); returns
+    (edges/s, rows, seconds, threads)."""
+    row_s = cpu_row_seconds(N, L, bias)
+    rows = int(min(20000, max(16, budget_s / row_s)))
+    secs, _, threads = cpu_port(N, L, bias, [rows])
+    return rows * NNZ * N * L / float(secs[0]), rows, float(secs[0]), threads
 
 
 def run_reference(args):
-    import snicit_gb300 as sg
+    import numpy as np
     if args.workload in UNEVEN:
-        import numpy as np
         N, L, bias, nb, lo, hi = UNEVEN[args.workload]
         rng = np.random.default_rng([SEED, 6])
         B = int(np.clip(np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), nb))), lo, hi).sum())
@@ -147,22 +154,18 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    layers = make_layers_csr(sg, N, L)
-    rates = []
-    rows = secs = threads = 0
-    # bounded samples: about 2.5 minutes of CPU work over the timed steps and
-    # 12 s over the warm-up ones, whatever K and W are (at most 12 s a step)
+    # bounded samples: about 2.5 minutes of host work over the timed steps and
+    # 12 s over the warm-up ones, whatever K and W are (at most 12 s a step);
+    # every step is its own group of consecutive rows of the workload's batch
+    row_s = cpu_row_seconds(N, L, bias)
     timed = min(12.0, max(1.0, 150.0 / max(1, args.steps)))
     warm = min(4.0, max(0.5, 12.0 / max(1, args.warmup)))
-    row_s = None  # measured once, by the first step's probe
-    for step in range(args.warmup + args.steps):
-        budget = warm if step < args.warmup else timed
-        r, rows, secs, threads, _ = cpu_port_rate(sg, N, L, bias, budget, offset=step * 997,
-                                                  layers=layers, row_s=row_s)
-        row_s = secs / rows
-        if step >= args.warmup:
-            rates.append(r)
-    value = statistics.median(rates)
+    sizes = [int(max(16, min(20000, (warm if i < args.warmup else timed) / row_s)))
+             for i in range(args.warmup + args.steps)]
+    secs, surv, threads = cpu_port(N, L, bias, sizes)
+    rates = [n * NNZ * N * L / max(float(t), 1e-9) for n, t in zip(sizes, secs)]
+    value = statistics.median(rates[args.warmup:])
+    rows = int(np.median(sizes[args.warmup:]))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "edges/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -170,12 +173,14 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "neurons": N, "layers": L, "batch": B,
                    "nnz_per_row": NNZ, "bias": bias, "mode": "plain recurrence (bf_inference)",
-                   "note": "ms_per_step extrapolated from the bounded sample"},
+                   "note": "ms_per_step extrapolated from the bounded sample to the whole batch"},
         "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows} rows of the {B}-row batch per step, all {L} layers, "
-                                   f"{secs:.1f} s; the reference has no CPU recurrence "
-                                   "(src/SDGC/utils/header.h:7-10), so this is the oracle's FP32 "
-                                   "restatement of bf_inference"},
+                         "sample": f"{rows} consecutive rows of the {B}-row batch per step "
+                                   f"({sum(surv[args.warmup:])} survivors over the timed steps), "
+                                   f"all {L} layers, median {statistics.median(secs[args.warmup:]):.1f} s "
+                                   "of layer arithmetic per step; the reference has no CPU "
+                                   "recurrence (src/SDGC/utils/header.h:7-10), so this is the "
+                                   "oracle's FP32 restatement of bf_inference"},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -377,10 +382,10 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        r, rows, secs, threads, _ = cpu_port_rate(sg, N, L, bias, args.cpu_seconds)
+        r, rows, secs, threads = cpu_port_rate(N, L, bias, args.cpu_seconds)
         cpu = {"value": r, "unit": "edges/s", "cores": threads, "kind": "port",
-               "sample": f"first {rows} rows of the batch, all {L} layers, {secs:.1f} s "
-                         "(FP32 restatement of bf_inference)"}
+               "sample": f"first {rows} rows of the batch, all {L} layers, {secs:.1f} s of "
+                         "layer arithmetic (FP32 restatement of bf_inference)"}
 
     if rank == 0:
         line = {

@@ -203,12 +203,6 @@ int sdnn_finalize_weights(sdnn_engine* e);
 int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows,
                     int32_t* flags, int32_t* ids, int64_t* count);
 
-/* Device-resident inference on the engine's stream (cudaStream_t passed as
- * void*; NULL = the engine's own).  d_Y0 rows x N FP32 device pointer
- * (16-byte aligned), d_flags rows int32 device pointer.  Plain modes do not
- * synchronize; SNICIT waits once, after the threshold clustering, to read how
- * many residue rows and centroids it produced (which picks the kernels for the
- * remaining layers). */
 /* The same with one-bit input rows (entry j of a row in bit j % 64 of word
  * j / 64, ceil(N / 64) words per row -- the layout of the bit-encoded input
  * files): 32x fewer bytes over the host link for 0/1 inputs such as the SDGC
@@ -216,6 +210,16 @@ int sdnn_infer_host(sdnn_engine* e, const float* Y0, int64_t rows,
 int sdnn_infer_host_bits(sdnn_engine* e, const uint64_t* bits, int64_t rows, int32_t* flags,
                          int32_t* ids, int64_t* count);
 
+/* Device-resident inference on the engine's stream (cudaStream_t passed as
+ * void*; NULL = the engine's own).  d_Y0 rows x N FP32 device pointer
+ * (16-byte aligned), d_flags rows int32 device pointer.  Every mode enqueues
+ * the whole inference without a host synchronisation: SNICIT is one CUDA
+ * graph launch in which a one-thread kernel reads how many residue rows and
+ * centroids the threshold clustering left and sets the graph's SWITCH node,
+ * which picks the post-threshold kernels on the device.  (With
+ * SDNN_FLAG_HOST_POST_CHOICE the host reads those counts back instead: one
+ * synchronisation after the clustering.)  The call returns once the work is
+ * enqueued; sdnn_get_stats waits for it. */
 int sdnn_infer_device(sdnn_engine* e, const float* d_Y0, int64_t rows,
                       int32_t* d_flags, void* stream);
 
@@ -284,19 +288,30 @@ int sdnn_get_layer_rows(const sdnn_engine* e, int64_t* out, int32_t num_layers);
 /* One plain layer (bias + ReLU + clamp) of an engine whose weights are already
  * on the device, applied to `rows` caller-owned rows: d_y_in (rows x N FP32,
  * 16-byte aligned) -> d_y_out (rows x N), d_alive[r] = 1 if row r has an
- * output > 0.  Allocates no memory at all; has no counterpart in the
+ * output > 0, else 0.  Allocates no memory at all; has no counterpart in the
  * reference.  For callers that cannot call cudaMalloc (during CUDA-graph
  * capture, fixed-budget or real-time serving threads, hosts whose allocator
  * belongs to another framework).  Its scratch is a static device array for
  * at most 65536 rows (larger `rows` -> SDNN_ERR_INVALID), shared by all calls
  * on a device: calls that overlap on the GPU race.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress); make it before
- * any stream capture.  Rows are in the engine's storage order: neuron order
- * for layer 0's input, and for every layer when the engine was created with
- * SDNN_FLAG_NO_PLACEMENT.  Requires sdnn_finalize_weights (or an inference)
- * first; stream NULL = the engine's stream; does not synchronise. */
+ * any stream capture.  d_y_in and d_y_out must not overlap (SDNN_ERR_INVALID):
+ * the layer is not computed in place.  Rows are in the engine's storage order:
+ * neuron order for layer 0's input, and for every layer when the engine was
+ * created with SDNN_FLAG_NO_PLACEMENT.  Requires sdnn_finalize_weights (or an
+ * inference) first; stream NULL = the engine's stream; does not synchronise;
+ * the caller's current device is left as it was.  Failure on the device: if a
+ * bounded device wait of the layer gives up, every d_alive entry is -1 after
+ * the call's work has run (check it once the stream is synchronised). */
 int sdnn_layer_noalloc(sdnn_engine* e, int32_t layer, const float* d_y_in, float* d_y_out,
                        int64_t rows, int32_t* d_alive, void* stream);
+
+/* Self-test of sdnn_layer_noalloc's failure report (no reference counterpart):
+ * runs its call sequence with the layer replaced by a device wait that nothing
+ * completes (bounded by limit_us <= 10 s), so every d_alive entry (rows of
+ * them) must read -1 afterwards; the engine and the scratch stay usable. */
+int sdnn_selftest_noalloc_timeout(sdnn_engine* e, int32_t* d_alive, int64_t rows,
+                                  int64_t limit_us, void* stream);
 
 /* Chooses threshold, centroid count and tile shape by timing the candidates
  * on the given sample rows (host buffer) and appends one JSON line per tried

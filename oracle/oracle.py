@@ -36,6 +36,20 @@ def lib():
         L.oracle_snicit.restype = ctypes.c_int
         L.oracle_ref_candidates.argtypes = [P, ctypes.c_int64, ctypes.c_int, ctypes.c_int, P]
         L.oracle_ref_candidates.restype = ctypes.c_int
+        L.oracle_gen_inputs.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int64,
+                                        ctypes.c_int64, P]
+        L.oracle_gen_inputs.restype = ctypes.c_int
+        L.oracle_gen_layer_csr.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_float, P, P, P]
+        L.oracle_gen_layer_csr.restype = ctypes.c_int
+        L.oracle_port_stream.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                         ctypes.c_float, ctypes.c_float, ctypes.c_float, P,
+                                         ctypes.c_int64, P, ctypes.c_int, ctypes.c_int, P, P]
+        L.oracle_port_stream.restype = ctypes.c_int
+        L.oracle_infer_stream64.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                            ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                            ctypes.c_float, P, ctypes.c_int64, ctypes.c_int, P, P]
+        L.oracle_infer_stream64.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -132,3 +146,59 @@ def head(Y, head_w, head_b):
     (dense_output, src/beyond/general.hpp:74-102); argmax = first maximum."""
     logits = np.asarray(Y, np.float64) @ np.asarray(head_w, np.float64) + np.asarray(head_b, np.float64)
     return logits, np.argmax(logits, axis=1).astype(np.int32)
+
+
+def gen_inputs(N, seed, row_offset, rows):
+    """Seeded 0/1 input rows of the synthetic SDGC workload (restated generator)."""
+    out = np.zeros((rows, N), dtype=np.float32)
+    if lib().oracle_gen_inputs(int(N), int(seed), int(row_offset), int(rows), _p(out)):
+        raise RuntimeError("oracle_gen_inputs failed")
+    return out
+
+
+def gen_layer_csr(N, seed, layer, nnz=32, value=0.0625):
+    """One synthetic layer as CSR by input row (restated generator)."""
+    ro = np.zeros(N + 1, dtype=np.int32)
+    cols = np.zeros(N * nnz, dtype=np.int32)
+    vals = np.zeros(N * nnz, dtype=np.float32)
+    if lib().oracle_gen_layer_csr(int(N), int(seed), int(layer), int(nnz), float(value), _p(ro),
+                                  _p(cols), _p(vals)):
+        raise RuntimeError("oracle_gen_layer_csr failed")
+    return ro, cols, vals
+
+
+def port_stream(N, L, seed, bias, Y0, group_sizes, nnz=32, value=0.0625, clamp=32.0,
+                nthreads=None):
+    """FP32 port of bf_inference on the synthetic net, weights generated layer
+    by layer; rows split into consecutive groups of the given sizes.  Returns
+    (alive, seconds per group of layer arithmetic, final activations)."""
+    Y = np.ascontiguousarray(Y0, dtype=np.float32).copy()
+    sizes = np.asarray(group_sizes, dtype=np.int64)
+    off = np.ascontiguousarray(np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64))
+    assert off[-1] == Y.shape[0]
+    alive = np.zeros(Y.shape[0], dtype=np.int32)
+    secs = np.zeros(len(sizes), dtype=np.float64)
+    if nthreads is None:
+        nthreads = os.cpu_count() or 1
+    rc = lib().oracle_port_stream(int(N), int(L), int(seed), int(nnz), float(value), float(bias),
+                                  float(clamp), _p(Y), Y.shape[0], _p(off), len(sizes),
+                                  int(nthreads), _p(alive), _p(secs))
+    if rc:
+        raise RuntimeError(f"oracle_port_stream failed ({rc})")
+    return alive, secs, Y
+
+
+def infer_stream64(N, L, seed, bias, Y0, nnz=32, value=0.0625, clamp=32.0, nthreads=None):
+    """FP64 oracle of the synthetic net (weights generated layer by layer);
+    returns (Y float64, alive)."""
+    Y0 = np.ascontiguousarray(Y0, dtype=np.float32)
+    Y = np.zeros(Y0.shape, dtype=np.float64)
+    alive = np.zeros(Y0.shape[0], dtype=np.int32)
+    if nthreads is None:
+        nthreads = os.cpu_count() or 1
+    rc = lib().oracle_infer_stream64(int(N), int(L), int(seed), int(nnz), float(value),
+                                     float(bias), float(clamp), _p(Y0), Y0.shape[0],
+                                     int(nthreads), _p(Y), _p(alive))
+    if rc:
+        raise RuntimeError(f"oracle_infer_stream64 failed ({rc})")
+    return Y, alive

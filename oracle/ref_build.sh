@@ -3,10 +3,11 @@
 # Compiles the reference's SDGC kernel headers, where they lie in the
 # reference tree, into device code under oracle/_ref/ (git-ignored):
 #   oracle/_ref/sdgc_ref.cubin   sm_103a cubin
-#   oracle/_ref/sdgc_ref.ptx     same kernels as PTX (loaded if the cubin is absent)
 # No reference source is copied.  Usage: oracle/ref_build.sh [REFERENCE_ROOT]
+# (the root is the argument, else $SNICIT_REFERENCE_ROOT, else the reference
+# mount of the build container, /root/reference)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${SNICIT_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 NVCC="${NVCC:-/usr/local/cuda/bin/nvcc}"
@@ -18,5 +19,4 @@ mkdir -p "$OUT"
 FLAGS=(-std=c++17 --extended-lambda -O3 -w -I "$REF/src/SDGC" -I "$REF/3rd-party")
 "$NVCC" "${FLAGS[@]}" -cubin -gencode arch=compute_103a,code=sm_103a \
   "$HERE/ref_kernels.cu" -o "$OUT/sdgc_ref.cubin"
-"$NVCC" "${FLAGS[@]}" -ptx -arch=compute_103a "$HERE/ref_kernels.cu" -o "$OUT/sdgc_ref.ptx"
 echo "$OUT/sdgc_ref.cubin"

@@ -73,7 +73,7 @@ static CUfunction find_kernel(CUmodule mod, const char* needle) {
 
 int main(int argc, char** argv) {
   if (argc < 4) {
-    std::fprintf(stderr, "usage: ref_harness <module.cubin|.ptx> <in.bin> <out.bin>\n");
+    std::fprintf(stderr, "usage: ref_harness <module.cubin> <in.bin> <out.bin>\n");
     return 1;
   }
   FILE* f = std::fopen(argv[2], "rb");

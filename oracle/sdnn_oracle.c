@@ -39,14 +39,31 @@
  *                      (src/SDGC/SNICIT/kernel.hpp:138-153, including the
  *                      overlapping bins for N > 1024), greedy pruning with
  *                      eps = 0.03 (centroid_sel, kernel.hpp:156-194).
+ *   oracle_gen_*       restatement of the synthetic SDGC data (counter-based
+ *                      SplitMix64 streams keyed by (seed, kind, layer/row), Steele
+ *                      et al., OOPSLA 2014): the same rows and weight columns as the
+ *                      engine's own generator, so the CPU baseline and the
+ *                      reference arm of the benchmark need nothing from the product.
+ *   oracle_port_stream the FP32 port of bf_inference (same arithmetic as
+ *                      oracle_infer precision 32) over row groups with the
+ *                      synthetic weights generated layer by layer, so a
+ *                      1920-layer net never sits in host memory whole; per group
+ *                      it times the layer arithmetic only (not the weight
+ *                      generation), like the reference's own timers around the
+ *                      layer loop (src/SDGC/BF/BF.hpp:159,217-219).
+ *   oracle_infer_stream64   the FP64 oracle of the synthetic net with the
+ *                      weights generated layer by layer (the 1920-layer nets'
+ *                      weights are 32 GB as CSR; this holds one layer).
  *
  * Parity pins: the golden fixtures under tests/golden/ (outputs of the
  * reference's own bf_inference / snig_inference kernels, compiled from its
  * sources and run on a GB300) are checked against oracle_infer by the CPU
  * tests.
  */
+#define _POSIX_C_SOURCE 200809L
 #include <math.h>
 #include <pthread.h>
+#include <time.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -404,6 +421,306 @@ int oracle_ref_candidates(const float* Ylive, int64_t live_rows, int N, int samp
   for (int s = 0; s < sample; ++s)
     if (keep[s]) out[n++] = s;
   return n;
+}
+
+/* ---- synthetic data (restatement of the engine's generator) ------------- */
+
+static uint64_t sm_fin(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+#define SM_GOLDEN 0x9E3779B97F4A7C15ull
+static uint64_t sm_key(uint64_t seed, uint64_t kind, uint64_t a, uint64_t b) {
+  uint64_t k = sm_fin(seed + SM_GOLDEN);
+  k = sm_fin(k ^ (kind * 0xD1B54A32D192ED03ull + SM_GOLDEN));
+  k = sm_fin(k ^ (a * 0xABC98388FB8FAC03ull + SM_GOLDEN));
+  k = sm_fin(k ^ (b * 0x8CB92BA72F3D8DD7ull + SM_GOLDEN));
+  return k;
+}
+static uint64_t sm_draw(uint64_t key, uint64_t i) { return sm_fin(key + (i + 1) * SM_GOLDEN); }
+/* high 64 bits of u * n, from 32-bit halves (no 128-bit type needed) */
+static uint32_t sm_bounded(uint64_t u, uint32_t n) {
+  const uint64_t lo = (u & 0xffffffffull) * n, hi = (u >> 32) * n;
+  return (uint32_t)((hi + (lo >> 32)) >> 32);
+}
+static double sm_unit53(uint64_t u) { return (double)(u >> 11) * (1.0 / 9007199254740992.0); }
+static int cmp_u64(const void* a, const void* b) {
+  const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* Columns of input row `row` of `layer`: nnz distinct outputs in draw order. */
+static void gen_row_cols(uint64_t seed, int layer, int row, int N, int nnz, int32_t* cols) {
+  const uint64_t key = sm_key(seed, 1, (uint64_t)layer, (uint64_t)row);
+  int have = 0;
+  for (uint64_t i = 0; have < nnz; ++i) {
+    const int32_t c = (int32_t)sm_bounded(sm_draw(key, i), (uint32_t)N);
+    int dup = 0;
+    for (int k = 0; k < have; ++k)
+      if (cols[k] == c) {
+        dup = 1;
+        break;
+      }
+    if (!dup) cols[have++] = c;
+  }
+}
+
+/* Seeded 0/1 input rows [row_offset, row_offset + rows): row density
+ * 0.95 * (2nd smallest of 9 uniforms), entries 1 with that probability. */
+int oracle_gen_inputs(int N, uint64_t seed, int64_t row_offset, int64_t rows, float* out) {
+  if (N <= 0 || rows < 0 || row_offset < 0 || (!out && rows > 0)) return 1;
+  for (int64_t r = 0; r < rows; ++r) {
+    const uint64_t key = sm_key(seed, 2, 0, (uint64_t)(row_offset + r));
+    uint64_t u[9];
+    for (int i = 0; i < 9; ++i) u[i] = sm_draw(key, (uint64_t)i) >> 11;
+    qsort(u, 9, sizeof(uint64_t), cmp_u64);
+    const double rho = 0.95 * ((double)u[1] * (1.0 / 9007199254740992.0));
+    float* o = out + r * (int64_t)N;
+    for (int j = 0; j < N; ++j) o[j] = sm_unit53(sm_draw(key, 9 + (uint64_t)j)) < rho ? 1.f : 0.f;
+  }
+  return 0;
+}
+
+/* One synthetic layer as CSR by input row: row_off[N+1], cols/vals N*nnz
+ * (columns in draw order; all distinct, so no duplicates to sum). */
+int oracle_gen_layer_csr(int N, uint64_t seed, int layer, int nnz, float value, int32_t* row_off,
+                         int32_t* cols, float* vals) {
+  if (N <= 0 || nnz <= 0 || nnz > N || layer < 0) return 1;
+  for (int i = 0; i <= N; ++i) row_off[i] = i * nnz;
+  for (int i = 0; i < N; ++i) {
+    gen_row_cols(seed, layer, i, N, nnz, cols + (int64_t)i * nnz);
+    for (int k = 0; k < nnz; ++k) vals[(int64_t)i * nnz + k] = value;
+  }
+  return 0;
+}
+
+/* ---- FP32 port over groups of rows, weights generated layer by layer ---- */
+
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+typedef struct {
+  int N, L, nnz, ngroups, nthreads;
+  uint64_t seed;
+  float wval, bias, clampv;
+  float* y;                 /* rows * N, updated in place */
+  int64_t rows;
+  const int64_t* group_off; /* ngroups + 1 row offsets */
+  int32_t* live;            /* rows */
+  int32_t* cols;            /* N * nnz of the current layer */
+  int layer;
+  int64_t next;             /* work counter of the current phase */
+  double* secs;             /* ngroups */
+  pthread_barrier_t bar;
+} stream_job;
+
+typedef struct {
+  stream_job* j;
+  int t;
+} stream_arg;
+
+static void* stream_worker(void* p) {
+  stream_arg* a = (stream_arg*)p;
+  stream_job* j = a->j;
+  const int N = j->N, nnz = j->nnz, T = j->nthreads;
+  float* acc = (float*)malloc(sizeof(float) * (size_t)N);
+  for (int l = 0; l < j->L; ++l) {
+    /* weights of layer l: input rows split over the threads (untimed) */
+    for (int i = (int)((int64_t)N * a->t / T); i < (int)((int64_t)N * (a->t + 1) / T); ++i)
+      gen_row_cols(j->seed, l, i, N, nnz, j->cols + (int64_t)i * nnz);
+    pthread_barrier_wait(&j->bar);
+    for (int g = 0; g < j->ngroups; ++g) {
+      double t0 = 0.0;
+      if (a->t == 0) {
+        __atomic_store_n(&j->next, j->group_off[g], __ATOMIC_SEQ_CST);
+        t0 = now_s();
+      }
+      pthread_barrier_wait(&j->bar);
+      for (;;) {
+        const int64_t r = __atomic_fetch_add(&j->next, 1, __ATOMIC_SEQ_CST);
+        if (r >= j->group_off[g + 1]) break;
+        if (!j->live[r]) continue;
+        float* y = j->y + r * (int64_t)N;
+        memset(acc, 0, sizeof(float) * (size_t)N);
+        for (int i = 0; i < N; ++i) {
+          const float v = y[i];
+          if (v == 0.f) continue;
+          const int32_t* co = j->cols + (int64_t)i * nnz;
+          for (int k = 0; k < nnz; ++k) {
+            const float prod = v * j->wval;
+            acc[co[k]] = acc[co[k]] + prod;
+          }
+        }
+        int any = 0;
+        for (int c = 0; c < N; ++c) {
+          const float v = acc[c] + j->bias;
+          if (v > 0.f) any = 1;
+          y[c] = v < 0.f ? 0.f : (v > j->clampv ? j->clampv : v);
+        }
+        if (!any) j->live[r] = 0;
+      }
+      pthread_barrier_wait(&j->bar);
+      if (a->t == 0) j->secs[g] += now_s() - t0;
+    }
+  }
+  free(acc);
+  return NULL;
+}
+
+/* FP32 plain recurrence (the arithmetic of oracle_infer precision 32) of the
+ * synthetic net (seed, nnz distinct columns per input row, every value wval,
+ * scalar bias) over the rows of Y (rows x N, overwritten with the final
+ * activations).  Rows [group_off[g], group_off[g+1]) form group g; secs[g]
+ * receives the wall time of group g's layer arithmetic summed over the
+ * layers (all threads on one group at a time).  alive_out[r] = 1 if row r
+ * survives every layer. */
+int oracle_port_stream(int N, int L, uint64_t seed, int nnz, float wval, float bias, float clampv,
+                       float* Y, int64_t rows, const int64_t* group_off, int ngroups,
+                       int nthreads, int32_t* alive_out, double* secs) {
+  if (N <= 0 || L < 0 || nnz <= 0 || nnz > N || !Y || rows < 0 || ngroups <= 0 || !group_off ||
+      group_off[0] != 0 || group_off[ngroups] != rows || !secs)
+    return 1;
+  if (nthreads < 1) nthreads = 1;
+  stream_job j;
+  memset(&j, 0, sizeof(j));
+  j.N = N;
+  j.L = L;
+  j.nnz = nnz;
+  j.ngroups = ngroups;
+  j.nthreads = nthreads;
+  j.seed = seed;
+  j.wval = wval;
+  j.bias = bias;
+  j.clampv = clampv;
+  j.y = Y;
+  j.rows = rows;
+  j.group_off = group_off;
+  j.secs = secs;
+  j.live = (int32_t*)malloc(sizeof(int32_t) * (size_t)(rows > 0 ? rows : 1));
+  j.cols = (int32_t*)malloc(sizeof(int32_t) * (size_t)N * (size_t)nnz);
+  /* every row enters layer 0 (an all-zero row dies there, BF.hpp:222-229) */
+  for (int64_t r = 0; r < rows; ++r) j.live[r] = 1;
+  for (int g = 0; g < ngroups; ++g) secs[g] = 0.0;
+  pthread_barrier_init(&j.bar, NULL, (unsigned)nthreads);
+  pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+  stream_arg* args = (stream_arg*)calloc((size_t)nthreads, sizeof(stream_arg));
+  for (int t = 0; t < nthreads; ++t) {
+    args[t].j = &j;
+    args[t].t = t;
+    if (t > 0) pthread_create(&th[t], NULL, stream_worker, &args[t]);
+  }
+  stream_worker(&args[0]);
+  for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+  pthread_barrier_destroy(&j.bar);
+  for (int64_t r = 0; r < rows; ++r) {
+    if (alive_out) alive_out[r] = j.live[r];
+    if (!j.live[r]) memset(Y + r * (int64_t)N, 0, sizeof(float) * (size_t)N);
+  }
+  free(th);
+  free(args);
+  free(j.live);
+  free(j.cols);
+  return 0;
+}
+
+/* ---- FP64 oracle with the weights generated layer by layer -------------- */
+
+typedef struct {
+  int N, L, nnz, nthreads;
+  uint64_t seed;
+  double wval, bias, clampv;
+  double* y;       /* rows * N */
+  int64_t rows;
+  int32_t* live;
+  int32_t* cols;
+  int64_t next;
+  pthread_barrier_t bar;
+} stream64_job;
+
+static void* stream64_worker(void* p) {
+  stream_arg* a = (stream_arg*)p;
+  stream64_job* j = (stream64_job*)a->j;
+  const int N = j->N, nnz = j->nnz, T = j->nthreads;
+  double* acc = (double*)malloc(sizeof(double) * (size_t)N);
+  for (int l = 0; l < j->L; ++l) {
+    for (int i = (int)((int64_t)N * a->t / T); i < (int)((int64_t)N * (a->t + 1) / T); ++i)
+      gen_row_cols(j->seed, l, i, N, nnz, j->cols + (int64_t)i * nnz);
+    if (a->t == 0) __atomic_store_n(&j->next, 0, __ATOMIC_SEQ_CST);
+    pthread_barrier_wait(&j->bar);
+    for (;;) {
+      const int64_t r = __atomic_fetch_add(&j->next, 1, __ATOMIC_SEQ_CST);
+      if (r >= j->rows) break;
+      if (!j->live[r]) continue;
+      double* y = j->y + r * (int64_t)N;
+      memset(acc, 0, sizeof(double) * (size_t)N);
+      for (int i = 0; i < N; ++i) {
+        const double v = y[i];
+        if (v == 0.0) continue;
+        const int32_t* co = j->cols + (int64_t)i * nnz;
+        for (int k = 0; k < nnz; ++k) acc[co[k]] += v * j->wval;
+      }
+      int any = 0;
+      for (int c = 0; c < N; ++c) {
+        const double v = acc[c] + j->bias;
+        if (v > 0.0) any = 1;
+        y[c] = v < 0.0 ? 0.0 : (v > j->clampv ? j->clampv : v);
+      }
+      if (!any) j->live[r] = 0;
+    }
+    pthread_barrier_wait(&j->bar);
+  }
+  free(acc);
+  return NULL;
+}
+
+/* The FP64 oracle (oracle_infer precision 64 arithmetic) of the synthetic
+ * net, weights generated layer by layer: Y64 (rows x N) receives the final
+ * activations (zero rows for dead samples), alive_out the categories. */
+int oracle_infer_stream64(int N, int L, uint64_t seed, int nnz, float wval, float bias,
+                          float clampv, const float* Y0, int64_t rows, int nthreads, double* Y64,
+                          int32_t* alive_out) {
+  if (N <= 0 || L < 0 || nnz <= 0 || nnz > N || !Y0 || rows < 0 || !Y64) return 1;
+  if (nthreads < 1) nthreads = 1;
+  stream64_job j;
+  memset(&j, 0, sizeof(j));
+  j.N = N;
+  j.L = L;
+  j.nnz = nnz;
+  j.nthreads = nthreads;
+  j.seed = seed;
+  j.wval = (double)wval;
+  j.bias = (double)bias;
+  j.clampv = (double)clampv;
+  j.y = Y64;
+  j.rows = rows;
+  for (int64_t i = 0; i < rows * (int64_t)N; ++i) Y64[i] = (double)Y0[i];
+  j.live = (int32_t*)malloc(sizeof(int32_t) * (size_t)(rows > 0 ? rows : 1));
+  j.cols = (int32_t*)malloc(sizeof(int32_t) * (size_t)N * (size_t)nnz);
+  for (int64_t r = 0; r < rows; ++r) j.live[r] = 1;
+  pthread_barrier_init(&j.bar, NULL, (unsigned)nthreads);
+  pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+  stream_arg* args = (stream_arg*)calloc((size_t)nthreads, sizeof(stream_arg));
+  for (int t = 0; t < nthreads; ++t) {
+    args[t].j = (stream_job*)&j;
+    args[t].t = t;
+    if (t > 0) pthread_create(&th[t], NULL, stream64_worker, &args[t]);
+  }
+  stream64_worker(&args[0]);
+  for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+  pthread_barrier_destroy(&j.bar);
+  for (int64_t r = 0; r < rows; ++r) {
+    if (alive_out) alive_out[r] = j.live[r];
+    if (!j.live[r]) memset(Y64 + r * (int64_t)N, 0, sizeof(double) * (size_t)N);
+  }
+  free(th);
+  free(args);
+  free(j.live);
+  free(j.cols);
+  return 0;
 }
 
 #ifdef __cplusplus

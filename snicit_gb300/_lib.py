@@ -112,6 +112,7 @@ SIGNATURES = [
     ("sdnn_save_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_load_packed_weights", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_layer_noalloc", ctypes.c_int, [P, I32, P, P, I64, P, P]),
+    ("sdnn_selftest_noalloc_timeout", ctypes.c_int, [P, P, I64, I64, P]),
     ("sdnn_server_config_default", ctypes.c_int, [P]),
     ("sdnn_server_create", ctypes.c_int, [P, P, P, P, P]),
     ("sdnn_server_destroy", ctypes.c_int, [P]),

@@ -54,8 +54,6 @@ def main(out_dir):
     subprocess.run(["nvcc", "-O2", "-std=c++17", os.path.join(ROOT, "oracle", "ref_harness.cpp"),
                     "-o", harness, "-lcuda"], check=True)
     module = os.path.join(REF, "sdgc_ref.cubin")
-    if not os.path.exists(module):
-        module = os.path.join(REF, "sdgc_ref.ptx")
     for name, (N, L, B, sec, bias, nnz, wkind, ikind, seed) in CASES.items():
         layers, Y0 = make_case(N, L, B, nnz, wkind, ikind, seed)
         inp = os.path.join(out_dir, name + ".in.bin")

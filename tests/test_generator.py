@@ -91,3 +91,40 @@ def test_survival_fraction_is_inside_the_reseed_window():
     iid = (rng.random((300, N)) < 0.19).astype(np.float32)
     _, alive_iid, dead = orc.infer(layers, N, -0.3, iid, precision=32, want_y=False)
     assert alive_iid.sum() == 0 and dead.max() <= 4
+
+
+def test_oracle_generator_restates_the_engine_generator():
+    """The oracle's C restatement of the synthetic data (used by the CPU
+    baseline and the reference arm of the benchmark) gives the engine's bits."""
+    from oracle import oracle as orc
+    for N in (256, 4096, 65536):
+        assert np.array_equal(orc.gen_inputs(N, 2026, 12345, 3), sg.generate_inputs(N, 2026, 12345, 3))
+        ro, c, v = orc.gen_layer_csr(N, 20260101, 7)
+        r2, c2, v2 = sg.generate_layer_coo(N, 20260101, 7, 32, 0.0625)
+        assert np.array_equal(c, c2) and np.array_equal(v, v2)
+        assert np.array_equal(ro, np.arange(N + 1, dtype=np.int32) * 32)
+
+
+def test_streamed_port_equals_the_fp32_port():
+    """oracle_port_stream (weights generated per layer, rows in timed groups)
+    computes the same bits as oracle_infer's FP32 port."""
+    from oracle import oracle as orc
+    N, L, seed, bias = 1024, 30, 20260101, -0.3
+    Y0 = orc.gen_inputs(N, seed, 0, 300)
+    layers = [orc.gen_layer_csr(N, seed, l) for l in range(L)]
+    want, alive_w, _ = orc.infer(layers, N, bias, Y0, precision=32, nthreads=4)
+    alive, secs, Y = orc.port_stream(N, L, seed, bias, Y0, [100, 150, 50], nthreads=3)
+    assert np.array_equal(alive, alive_w)
+    assert np.array_equal(Y.view(np.uint32), want.view(np.uint32))
+    assert (secs > 0).all() and 0 < alive.sum() < 300
+
+
+def test_streamed_fp64_oracle_equals_the_fp64_oracle():
+    from oracle import oracle as orc
+    N, L, seed, bias = 512, 25, 20260101, -0.3
+    Y0 = orc.gen_inputs(N, seed, 0, 200)
+    layers = [orc.gen_layer_csr(N, seed, l) for l in range(L)]
+    want, alive_w, _ = orc.infer(layers, N, bias, Y0, precision=64, nthreads=4)
+    Y, alive = orc.infer_stream64(N, L, seed, bias, Y0, nthreads=3)
+    assert np.array_equal(alive, alive_w) and 0 < alive.sum() < 200
+    assert np.array_equal(Y, want)

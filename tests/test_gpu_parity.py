@@ -44,6 +44,10 @@ def _check(Y, flags, ids, Yref, alive, label, rtol=RTOL, Y32=None):
         tol = np.maximum(tol, 4.0 * _rel(Y32, Yref).max(axis=1))
     bad = np.flatnonzero(err > tol)
     assert len(bad) == 0, f"{label}: activation error {err[bad].max():.3g} > {tol[bad].min():.3g} on {len(bad)} rows"
+    loose = int((tol > rtol).sum())
+    print(f"{label}: max error {err.max():.3g}, largest per-row bound {tol.max():.3g} "
+          f"({loose} of {len(tol)} rows above {rtol:g})")
+    return float(tol.max())
 
 
 def _ref(layers, N, bias, Y0, **kw):
