@@ -329,9 +329,10 @@ typedef struct sdnn_server sdnn_server;
 typedef struct sdnn_server_config {
   int32_t slots;           /* passes in flight: one engine, stream and worker each */
   int32_t head_outputs;    /* width of the dense head after the last layer (0 = none) */
-  int64_t max_rows;        /* upper bound of rows per pass (0 = none; default 16384) */
-  double memory_fraction;  /* share of free device memory the slots may take: the
-                              rows per pass are what fits in it (default 0.25)     */
+  int64_t max_rows;        /* largest request and largest pass, in rows (0 = 2^20;
+                              default 16384)                                        */
+  double memory_fraction;  /* share of the device memory free at admission time that
+                              slots may grow into (default 0.25)                    */
   int64_t max_pending;     /* queued requests before sdnn_submit answers BUSY       */
   int64_t max_delay_us;    /* batching window: a pass that is not full waits until
                               its oldest request has queued this long (default 0) */
@@ -341,7 +342,8 @@ typedef struct sdnn_server_config {
 } sdnn_server_config;
 
 typedef struct sdnn_server_stats {
-  int64_t passes, rows, requests, max_rows_in_pass, queued, slot_rows;
+  int64_t passes, rows, requests, max_rows_in_pass, queued;
+  int64_t slot_rows;  /* rows the largest slot's buffers hold now */
   int32_t slots;
   int32_t reserved[7];
 } sdnn_server_stats;
@@ -349,20 +351,26 @@ typedef struct sdnn_server_stats {
 int sdnn_server_config_default(sdnn_server_config* cfg);
 
 /* A request server over the network of `model` (an engine with its weights
- * set; the server copies them into its own slot engines).  head_w is N x
- * head_outputs (row-major, by neuron), head_b has head_outputs entries: the
- * dense output layer of the beyond nets (src/beyond/general.hpp:74-102).
- * Requests arrive with sdnn_submit at any time and are admitted, in arrival
- * order, into the first free slot while they fit its row capacity; slots run
+ * set).  The slot engines read the model's device weights -- one copy on the
+ * device for every slot -- so the model must outlive the server and keep its
+ * weights: while a server uses them, the model's weight setters and
+ * sdnn_destroy answer SDNN_ERR_STATE.  head_w is N x head_outputs (row-major,
+ * by neuron), head_b has head_outputs entries: the dense output layer of the
+ * beyond nets (src/beyond/general.hpp:74-102).  Requests arrive with
+ * sdnn_submit at any time and are admitted, in arrival order, into the first
+ * free slot while they fit: a slot takes the rows its buffers hold plus what
+ * the device memory free at that moment (cudaMemGetInfo x memory_fraction,
+ * less what other slots were just granted) lets it grow by; a request that
+ * fits nowhere while no pass runs completes with SDNN_ERR_OOM.  Slots run
  * concurrently.  The reference has no serving loop; its beyond driver runs
  * fixed rounds (src/beyond/SNICIT/SNICIT.hpp:494-641). */
 int sdnn_server_create(sdnn_engine* model, const sdnn_server_config* cfg, const float* head_w,
                        const float* head_b, sdnn_server** out);
 int sdnn_server_destroy(sdnn_server* sv);
-/* Rows a slot holds (the largest admissible request). */
+/* The largest admissible request, in rows (max_rows). */
 int64_t sdnn_server_capacity(const sdnn_server* sv);
 /* Queues `rows` x N host floats (copied); SDNN_ERR_BUSY when the queue is full,
- * SDNN_ERR_INVALID when rows exceed the slot capacity. */
+ * SDNN_ERR_INVALID when rows exceed max_rows. */
 int sdnn_submit(sdnn_server* sv, const float* rows_host, int64_t rows, uint64_t* request_id);
 /* done = 1 when finished, then copies flags (rows), logits (rows x head),
  * argmax (rows) and the submit-to-completion latency in seconds (each

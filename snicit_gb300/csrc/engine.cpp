@@ -112,7 +112,10 @@ struct sdnn_engine {
   int threads = 512, grid = 0, grid_general = 0, min_split = 1;
   size_t smem = 0;
 
-  // device weights
+  // device weights (owned, or borrowed from weights_owner: a server's slot
+  // engines read the model engine's copy; share_users counts the borrowers)
+  const sdnn_engine* weights_owner = nullptr;
+  std::atomic<int> share_users{0};
   std::vector<DevLayer> dl;
   int64_t total_nnz = 0;
   // neuron placement: positions of the outputs of every layer (empty = identity)
@@ -233,6 +236,14 @@ void dfree(T*& p) {
 }
 
 void free_weights(sdnn_engine* e) {
+  if (e->weights_owner) {  // borrowed: the owner frees them
+    const_cast<sdnn_engine*>(e->weights_owner)->share_users.fetch_sub(1);
+    e->dl.clear();
+    e->d_perm_final = nullptr;
+    e->d_layer_table = nullptr;
+    e->weights_owner = nullptr;
+    return;
+  }
   dfree(e->d_perm_final);
   dfree(e->d_layer_table);
   for (auto& d : e->dl) {
@@ -1509,6 +1520,8 @@ int sdnn_create(const sdnn_config* cfg, sdnn_engine** out) {
 
 int sdnn_destroy(sdnn_engine* e) {
   if (!e) return SDNN_OK;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
   if (e->stream) {
     cudaSetDevice(e->dev);
     cudaStreamSynchronize(e->stream);
@@ -1533,6 +1546,8 @@ const char* sdnn_last_error(const sdnn_engine* e) { return e ? e->err.c_str() : 
 
 int sdnn_load_weights_tsv(sdnn_engine* e, const char* dir) {
   if (!e || !dir) return SDNN_ERR_INVALID;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
   e->gen.on = false;
   for (int l = 0; l < e->L; ++l) {
     const std::string p = std::string(dir) + "/n" + std::to_string(e->N) + "-l" +
@@ -1548,6 +1563,8 @@ int sdnn_load_weights_tsv(sdnn_engine* e, const char* dir) {
 int sdnn_set_layer_coo(sdnn_engine* e, int32_t layer, const int32_t* rows, const int32_t* cols,
                        const float* vals, int64_t nnz) {
   if (!e) return SDNN_ERR_INVALID;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
   if (layer < 0 || layer >= e->L || nnz < 0 || (nnz > 0 && (!rows || !cols || !vals)))
     return fail(e, SDNN_ERR_INVALID, "bad layer or arrays");
   if (e->gen.on) {
@@ -1567,6 +1584,8 @@ int sdnn_set_layer_coo(sdnn_engine* e, int32_t layer, const int32_t* rows, const
 
 int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias) {
   if (!e || !bias) return SDNN_ERR_INVALID;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
   if (layer < 0 || layer >= e->L) return fail(e, SDNN_ERR_INVALID, "bad layer");
   if (e->packed)
     return fail(e, SDNN_ERR_STATE, "weights come from a packed file (its biases are part of it)");
@@ -1578,6 +1597,8 @@ int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias) {
 
 int sdnn_generate_weights(sdnn_engine* e, uint64_t seed, int32_t nnz_per_row, float value) {
   if (!e) return SDNN_ERR_INVALID;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
   if (nnz_per_row < 1 || nnz_per_row > e->N) return fail(e, SDNN_ERR_INVALID, "bad nnz_per_row");
   e->packed.reset();
   e->gen.on = true;
@@ -1984,6 +2005,8 @@ int sdnn_save_packed_weights(sdnn_engine* e, const char* path) {
 
 int sdnn_load_packed_weights(sdnn_engine* e, const char* path) {
   if (!e || !path) return SDNN_ERR_INVALID;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
   std::string err;
   std::shared_ptr<PackedFile> pf = open_packed_file(path, err);
   if (!pf) return fail(e, err.rfind("cannot", 0) == 0 ? SDNN_ERR_IO : SDNN_ERR_FORMAT, err);
@@ -2132,12 +2155,30 @@ int engine_layer_setup(sdnn_engine* e, int layer, LayerArgs* a, LayerKernelKey* 
 cudaStream_t engine_stream(const sdnn_engine* e) { return e->stream; }
 
 // ---- hooks for the serving loop (serve.cpp)
-void engine_copy_weights(sdnn_engine* dst, const sdnn_engine* src) {
-  dst->packed = src->packed;
-  dst->gen = src->gen;
-  dst->hw = src->hw;
-  dst->hbias = src->hbias;
-  dst->weights_dirty = true;
+// The slot engines of a server read the model engine's device weights (one
+// copy on the device for every slot): src must have its weights on the device
+// and keep them (its weight setters and sdnn_destroy answer SDNN_ERR_STATE
+// while share_users > 0).
+int engine_share_weights(sdnn_engine* dst, sdnn_engine* src) {
+  int rc = ensure_cuda(src);
+  if (rc) return rc;
+  if ((rc = finalize_weights(src))) return rc;
+  if (dst->N != src->N || dst->L != src->L || dst->dev != src->dev)
+    return fail(dst, SDNN_ERR_INVALID, "shared weights: another shape or device");
+  drop_graph(dst);
+  free_weights(dst);
+  dst->dl = src->dl;
+  dst->pos = src->pos;
+  dst->d_perm_final = src->d_perm_final;
+  dst->d_layer_table = src->d_layer_table;
+  dst->total_nnz = src->total_nnz;
+  dst->chain_cap = src->chain_cap;
+  dst->chain_wcap8 = src->chain_wcap8;
+  dst->chain_wcap16 = src->chain_wcap16;
+  dst->weights_owner = src;
+  dst->weights_dirty = false;
+  src->share_users.fetch_add(1);
+  return SDNN_OK;
 }
 int engine_prepare(sdnn_engine* e, int64_t rows) { return prepare(e, rows); }
 float* engine_input(sdnn_engine* e) { return e->d_in; }

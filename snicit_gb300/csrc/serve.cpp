@@ -6,9 +6,13 @@
 //
 //  * sdnn_submit copies the request's rows into the server and queues it;
 //  * a dispatcher thread hands queued requests, in arrival order, to the first
-//    free slot while they fit its row capacity (sized from free device memory
-//    at creation, "admitted by free HBM");
-//  * each slot owns an engine (its stream, row buffers and weights) and a
+//    free slot while they fit: a slot holds the rows its buffers already have
+//    room for, plus what the device's free memory, read at that moment
+//    (cudaMemGetInfo, less what other slots are about to take), allows it to
+//    grow by ("admitted by free HBM"); the slot's worker grows its buffers
+//    before the pass;
+//  * each slot owns an engine (its stream and row buffers; the weights are
+//    the model engine's, one device copy for all slots) and a
 //    worker thread that runs one pass: the slot's requests gathered back to
 //    back, one inference over all their rows (in SNICIT mode the clustering
 //    spans every co-resident request), the dense head, results copied out;
@@ -37,7 +41,7 @@
 
 namespace sdnn {
 int engine_prepare(sdnn_engine* e, int64_t rows);
-void engine_copy_weights(sdnn_engine* dst, const sdnn_engine* src);
+int engine_share_weights(sdnn_engine* dst, sdnn_engine* src);
 sdnn_config engine_config(const sdnn_engine* e);
 cudaStream_t engine_stream(const sdnn_engine* e);
 float* engine_input(sdnn_engine* e);
@@ -68,6 +72,9 @@ struct Request {
 
 struct Slot {
   sdnn_engine* eng = nullptr;
+  int64_t cap = 0;        // rows the buffers below hold
+  int64_t grow_to = 0;    // set at admission: rows to grow to before the pass
+  int64_t reserved = 0;   // device bytes set aside for that growth
   float* h_in = nullptr;  // pinned staging: rows x N
   float* h_logits = nullptr;
   int32_t* h_argmax = nullptr;
@@ -84,7 +91,10 @@ struct Slot {
 struct sdnn_server {
   sdnn_server_config cfg{};
   int N = 0, H = 0;
-  int64_t cap = 0;
+  int64_t cap = 0;           // largest admissible request (rows)
+  int64_t per_row = 0;       // device bytes per row of a slot
+  int64_t reserved = 0;      // device bytes admitted but not yet allocated
+  sdnn_engine* model = nullptr;
   std::vector<std::unique_ptr<Slot>> slots;
   float* d_head = nullptr;  // head by final position, N x H
   float* d_hb = nullptr;
@@ -103,9 +113,63 @@ struct sdnn_server {
 
 namespace {
 
+// Grows a slot's row buffers (engine, pinned staging, head outputs) to `rows`.
+int grow_slot(sdnn_server* sv, Slot& slot, int64_t rows) {
+  if (rows <= slot.cap) return SDNN_OK;
+  const size_t N = (size_t)sv->N, H = (size_t)sv->H;
+  int rc = sdnn::engine_prepare(slot.eng, rows);
+  if (rc) return rc;
+  if (slot.h_in) cudaFreeHost(slot.h_in);
+  if (slot.h_flags) cudaFreeHost(slot.h_flags);
+  if (slot.h_logits) cudaFreeHost(slot.h_logits);
+  if (slot.h_argmax) cudaFreeHost(slot.h_argmax);
+  if (slot.d_logits) cudaFree(slot.d_logits);
+  if (slot.d_argmax) cudaFree(slot.d_argmax);
+  slot.h_in = slot.h_logits = nullptr;
+  slot.h_flags = slot.h_argmax = slot.d_argmax = nullptr;
+  slot.d_logits = nullptr;
+  slot.cap = 0;
+  bool ok = cudaMallocHost((void**)&slot.h_in, sizeof(float) * (size_t)rows * N) == cudaSuccess;
+  ok = ok && cudaMallocHost((void**)&slot.h_flags, sizeof(int32_t) * (size_t)rows) == cudaSuccess;
+  if (H > 0) {
+    ok = ok && cudaMallocHost((void**)&slot.h_logits, sizeof(float) * (size_t)rows * H) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&slot.h_argmax, sizeof(int32_t) * (size_t)rows) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&slot.d_logits, sizeof(float) * (size_t)rows * H) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&slot.d_argmax, sizeof(int32_t) * (size_t)rows) == cudaSuccess;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    return SDNN_ERR_OOM;
+  }
+  slot.cap = rows;
+  return SDNN_OK;
+}
+
 void run_pass(sdnn_server* sv, Slot& slot) {
   const int N = sv->N, H = sv->H;
   int64_t total = 0;
+  for (auto& r : slot.work) total += r->rows;
+  int grc = grow_slot(sv, slot, std::max(total, slot.grow_to));
+  {
+    std::lock_guard<std::mutex> lock(sv->mu);
+    sv->reserved -= slot.reserved;
+    slot.reserved = 0;
+    slot.grow_to = 0;
+  }
+  if (grc != SDNN_OK) {
+    const auto t = Clock::now();
+    std::lock_guard<std::mutex> lock(sv->mu);
+    for (auto& r : slot.work) {
+      r->status = grc;
+      r->t_start = r->t_done = t;
+      std::vector<float>().swap(r->in);
+      r->done = true;
+    }
+    slot.work.clear();
+    slot.busy = false;
+    return;
+  }
+  total = 0;
   for (auto& r : slot.work) {
     std::memcpy(slot.h_in + total * N, r->in.data(), sizeof(float) * (size_t)r->rows * N);
     total += r->rows;
@@ -193,24 +257,60 @@ void dispatcher_main(sdnn_server* sv) {
         continue;
       }
     }
+    bool admitted = false, any_busy = false;
+    for (auto& s : sv->slots) any_busy |= s->busy;
     for (auto& s : sv->slots) {
       if (s->busy || sv->queue.empty()) continue;
+      // rows this slot may take now: its buffers, plus what the free device
+      // memory (read now, less the growth other slots were granted) allows
+      int64_t allow = s->cap;
+      if (allow < sv->cap) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+          const double frac =
+              sv->cfg.memory_fraction > 0 ? std::min(sv->cfg.memory_fraction, 0.95) : 0.5;
+          const double avail = (double)free_b * frac - (double)sv->reserved;
+          if (avail > 0) allow += (int64_t)(avail / (double)sv->per_row);
+        }
+        allow = std::min(allow, sv->cap);
+      }
       int64_t rows = 0;
       const size_t max_req = sv->cfg.max_requests_per_pass > 0
                                  ? (size_t)sv->cfg.max_requests_per_pass
                                  : sv->queue.size();
       while (!sv->queue.empty() && s->work.size() < max_req &&
-             rows + sv->queue.front()->rows <= sv->cap) {
+             rows + sv->queue.front()->rows <= allow) {
         rows += sv->queue.front()->rows;
         s->work.push_back(sv->queue.front());
         sv->queue.pop_front();
       }
+      if (s->work.empty() && !any_busy && !admitted) {
+        // nothing fits and nothing runs that could free memory: the request
+        // is not admissible now (SDNN_ERR_OOM), rather than waiting forever
+        auto r = sv->queue.front();
+        sv->queue.pop_front();
+        sv->queued_rows -= r->rows;
+        r->status = SDNN_ERR_OOM;
+        r->t_start = r->t_done = Clock::now();
+        std::vector<float>().swap(r->in);
+        r->done = true;
+        sv->cv_done.notify_all();
+        continue;
+      }
       sv->queued_rows -= rows;
       if (!s->work.empty()) {
+        if (rows > s->cap) {
+          // grow a little ahead (up to twice the pass) while memory allows
+          s->grow_to = std::min(allow, std::max(rows, std::min(sv->cap, 2 * rows)));
+          s->reserved = (s->grow_to - s->cap) * sv->per_row;
+          sv->reserved += s->reserved;
+        }
         s->busy = true;
+        admitted = any_busy = true;
         sv->cv_slot.notify_all();
       }
     }
+    if (!admitted && !sv->queue.empty()) sv->cv_dispatch.wait(lock);
   }
 }
 
@@ -268,53 +368,26 @@ int sdnn_server_create(sdnn_engine* model, const sdnn_server_config* cfg, const 
     delete sv;
     return SDNN_ERR_CUDA;
   }
-  // slot capacity from free device memory: per row the input, two activation
-  // buffers and a few ints; capped at the per-row-list width of the kernels
-  int64_t cap = 0;
-  {
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
-      delete sv;
-      return SDNN_ERR_CUDA;
-    }
-    const double frac = cfg->memory_fraction > 0 ? std::min(cfg->memory_fraction, 0.9) : 0.25;
-    // device bytes per row of a slot: input, two layer buffers, the
-    // materialise scratch is one of them, row lists/state (~64 B), logits
-    const int64_t per_row = (int64_t)sv->N * 4 * 3 + 64 + (int64_t)sv->H * 4;
-    cap = (int64_t)((double)free_b * frac / cfg->slots / (double)per_row);
-    if (cfg->max_rows > 0) cap = std::min<int64_t>(cap, cfg->max_rows);
-    cap = std::min<int64_t>(cap, 1 << 20);
-  }
-  if (cap < 1) {
-    delete sv;
-    return SDNN_ERR_OOM;
-  }
-  sv->cap = cap;
+  // device bytes per row of a slot: input, two layer buffers (the
+  // materialise scratch is one of them), row lists/state (~64 B), logits
+  sv->per_row = (int64_t)sv->N * 4 * 3 + 64 + (int64_t)sv->H * 4;
+  sv->cap = cfg->max_rows > 0 ? std::min<int64_t>(cfg->max_rows, 1 << 20) : (1 << 20);
+  sv->model = model;
   sdnn_config ec = mc;
-  ec.batch = cap;
+  // slots start small and grow at admission, as free device memory allows
+  const int64_t initial = std::min<int64_t>(sv->cap, 4096);
+  ec.batch = initial;
   int rc = SDNN_OK;
   for (int i = 0; i < cfg->slots && rc == SDNN_OK; ++i) {
     auto slot = std::make_unique<Slot>();
     rc = sdnn_create(&ec, &slot->eng);
     if (rc == SDNN_OK) {
-      sdnn::engine_copy_weights(slot->eng, model);
-      rc = sdnn::engine_prepare(slot->eng, cap);
+      rc = sdnn::engine_share_weights(slot->eng, model);
       if (rc) sv->err = sdnn::engine_error(slot->eng);
     }
-    const size_t N = (size_t)sv->N, H = (size_t)sv->H;
     if (rc == SDNN_OK) {
-      bool ok = cudaMallocHost((void**)&slot->h_in, sizeof(float) * (size_t)cap * N) == cudaSuccess;
-      ok = ok && cudaMallocHost((void**)&slot->h_flags, sizeof(int32_t) * (size_t)cap) == cudaSuccess;
-      if (H > 0) {
-        ok = ok && cudaMallocHost((void**)&slot->h_logits, sizeof(float) * (size_t)cap * H) == cudaSuccess;
-        ok = ok && cudaMallocHost((void**)&slot->h_argmax, sizeof(int32_t) * (size_t)cap) == cudaSuccess;
-        ok = ok && cudaMalloc((void**)&slot->d_logits, sizeof(float) * (size_t)cap * H) == cudaSuccess;
-        ok = ok && cudaMalloc((void**)&slot->d_argmax, sizeof(int32_t) * (size_t)cap) == cudaSuccess;
-      }
-      if (!ok) {
-        cudaGetLastError();
-        rc = SDNN_ERR_OOM;
-      }
+      rc = grow_slot(sv, *slot, initial);
+      if (rc) sv->err = sdnn::engine_error(slot->eng);
     }
     sv->slots.push_back(std::move(slot));
   }
@@ -415,7 +488,7 @@ int sdnn_server_get_stats(sdnn_server* sv, sdnn_server_stats* out) {
   out->requests = sv->requests_done;
   out->max_rows_in_pass = sv->max_rows_in_pass;
   out->queued = (int64_t)sv->queue.size();
-  out->slot_rows = sv->cap;
+  for (auto& sl : sv->slots) out->slot_rows = std::max(out->slot_rows, sl->cap);
   out->slots = (int32_t)sv->slots.size();
   return SDNN_OK;
 }

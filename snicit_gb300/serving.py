@@ -50,6 +50,7 @@ class Server:
             hb = np.ascontiguousarray(head_b, dtype=np.float32)
             assert hw.shape == (self.N, self.H) and hb.shape == (self.H,)
         self._h = ctypes.c_void_p()
+        self._engine = engine  # the slots read its device weights: keep it alive
         engine._ck(lib.sdnn_server_create(engine._h, ctypes.byref(cfg),
                                           hw.ctypes.data if hw is not None else None,
                                           hb.ctypes.data if hb is not None else None,

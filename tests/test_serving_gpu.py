@@ -110,3 +110,57 @@ def test_admission_errors():
             with pytest.raises(SdnnError) as ei:
                 sv.submit(sg.mlp_inputs(seed, 2, 4))
             assert ei.value.code == 9
+
+
+def test_slots_share_the_model_weights_and_grow_at_admission():
+    """One device copy of the weights serves every slot: the model's weights
+    cannot change while a server reads them.  Slots start with buffers for
+    4096 rows and grow when a larger request is admitted (free device memory
+    read at admission); the results equal the model engine's own."""
+    N, seed = 1024, 23
+    layers, hw, hb = sg.sparse_mlp(seed, L=12)
+    big = sg.mlp_inputs(seed, 0, 10000)
+    small = sg.mlp_inputs(seed, 1, 37)
+    with _engine(layers, N) as eng:
+        f_big, _ = eng.infer(big)
+        y_big = eng.activations(len(big))
+        with sg.Server(eng, hw, hb, slots=3, max_rows=16384) as sv:
+            st0 = sv.stats()
+            assert st0["slot_rows"] == 4096
+            with pytest.raises(SdnnError) as ei:
+                eng.set_layer_csr(0, *layers[0])
+            assert ei.value.code == 6  # SDNN_ERR_STATE: in use by the server
+            r_small = sv.wait(sv.submit(small))
+            r_big = sv.wait(sv.submit(big))
+            st = sv.stats()
+        assert st["slot_rows"] >= len(big)
+        assert np.array_equal(r_big.flags, f_big)
+        lref, aref = orc.head(y_big, hw, hb)
+        assert _rel(r_big.logits, lref).max() <= 1e-5  # FP32 head of the same FP32 rows
+        assert r_small.flags.shape == (37,)
+        eng.set_layer_csr(0, *layers[0])  # the server is gone: allowed again
+
+
+def test_full_depth_argmax_on_clear_rows():
+    """The 120-layer serving net: FP32 cannot hold the logits to 1e-5 of FP64
+    at this depth (the recurrence amplifies rounding), so the argmax is
+    compared with the FP64 oracle on every row whose FP64 top-two margin
+    exceeds 4x the FP32 port's own logit error on that row -- there the answer
+    does not depend on rounding; the count of such rows is reported."""
+    N, seed = 1024, 31
+    layers, hw, hb = sg.sparse_mlp(seed)
+    x = sg.mlp_inputs(seed, 0, 2000)
+    with _engine(layers, N) as eng, sg.Server(eng, hw, hb, slots=2, max_rows=4096) as sv:
+        r = sv.wait(sv.submit(x))
+    Y, alive, _ = orc.infer(layers, N, -0.05, x, precision=64)
+    Y32, _, _ = orc.infer(layers, N, -0.05, x, precision=32)
+    lref, aref = orc.head(Y, hw, hb)
+    l32, _ = orc.head(Y32, hw, hb)
+    assert np.array_equal(r.flags, alive.astype(np.int32))
+    err32 = np.abs(l32 - lref).max(axis=1)
+    top2 = np.sort(lref, axis=1)[:, -2:]
+    clear = (top2[:, 1] - top2[:, 0]) > 4.0 * err32
+    print(f"120-layer net: {clear.sum()} of {len(x)} rows with a clear FP64 argmax; "
+          f"FP32 port logit error up to {err32.max():.3g}")
+    assert clear.sum() >= len(x) // 4
+    assert np.array_equal(r.argmax[clear], aref[clear])
