@@ -1,12 +1,16 @@
 #!/usr/bin/env python3
 """Headline benchmark: SNICIT-form SDGC inference on one GB300.
 
-Workload (default "sdgc-4096x480"): N=4096 neurons, L=480 layers, a batch of
-B=60000 seeded binary inputs (per-row density 0.95*Beta(2,8), mean 0.19),
-32 nonzeros per weight row at 0.0625, bias -0.35, clamp 32.  One step = one
+Workload (default "sdgc-65536x1920"): N=65536 neurons, L=1920 layers, a batch
+of B=60000 seeded binary inputs (per-row density 0.95*Beta(2,8), mean 0.19),
+32 nonzeros per weight row at 0.0625, bias -0.45, clamp 32.  One step = one
 full inference of the batch through the SNICIT path (plain layers up to the
-autotuned threshold, clustering, residue layers, recovery).  The plain
-per-layer path (SNIG mode) on the same batch is measured alongside.
+autotuned threshold, clustering, residue layers, recovery).  Measured beside
+it in the same run: the plain per-layer path (SNIG mode) on the same batch,
+the end-to-end host API, the dominant kernel alone (roofline), twelve uneven
+batches (log-uniform 500..60000 rows) in one launch schedule against one by
+one, the 4096 x 480 workload as an extra key, the serving loop, and the CPU
+baseline.
 
 Metric: nominal SDGC edges/s = B * 32 * N * L / t (the reference paper's
 throughput definition), plus ms per inference.
@@ -205,6 +209,90 @@ def load_weights(eng, args, N, L):
     return "generated + packed"
 
 
+def uneven_sizes(lo=500, hi=60000, nb=12):
+    """Twelve seeded batch sizes, log-uniform in [lo, hi]."""
+    import numpy as np
+    rng = np.random.default_rng([SEED, 6])
+    sizes = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), nb))).astype(np.int64)
+    return np.clip(sizes, lo, hi)
+
+
+def autotune(eng, args, name, d_ptr, rows):
+    if args.no_autotune or args.tile:
+        return None
+    rec = os.path.join(args.record_dir, f"autotune_{name}.jsonl")
+    os.makedirs(os.path.dirname(rec), exist_ok=True)
+    if os.path.exists(rec):
+        os.remove(rec)
+    eng.autotune_device(d_ptr, rows, rec)
+    return rec
+
+
+def time_steps(torch, stream, fn, steps):
+    """Device time of `steps` calls of fn on `stream` (CUDA events), per step too."""
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per = []
+    ev0.record(stream)
+    for _ in range(steps):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        fn()
+        s1.record(stream)
+        per.append((s0, s1))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), [a.elapsed_time(b) for a, b in per]
+
+
+def layer_kernel_roofline(torch, sg, eng, d_in, B, N, stream, peak, peak_kind, sm_mhz, args):
+    """The dominant kernel alone: layer 1 of the workload (the layer kernel over
+    every row of the batch, its inputs the layer-0 outputs) through the
+    no-allocation one-layer entry point, timed with CUDA events on the stream
+    it is launched on; algorithmic bytes = 8 B per row entry (read + write),
+    4 B per row id, 8 B per weight nonzero."""
+    import ctypes
+    lib = sg.load()
+    rows = min(B, 65536)
+    y1 = torch.empty((rows, N), dtype=torch.float32, device=d_in.device)
+    y2 = torch.empty_like(y1)
+    alive = torch.empty(rows, dtype=torch.int32, device=d_in.device)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def call(layer, src, dst):
+        rc = lib.sdnn_layer_noalloc(eng._h, layer, ctypes.c_void_p(src.data_ptr()),
+                                    ctypes.c_void_p(dst.data_ptr()), rows,
+                                    ctypes.c_void_p(alive.data_ptr()), sp)
+        assert rc == 0, lib.sdnn_last_error(eng._h)
+
+    call(0, d_in[:rows], y1)
+    for _ in range(3):
+        call(1, y1, y2)
+    n = max(3, min(args.steps, 10))
+    # inputs (rows x N x 4 B) are larger than L2 at every workload here
+    total_ms, per = time_steps(torch, stream, lambda: call(1, y1, y2), n)
+    ms = statistics.median(per)
+    nnz = NNZ * N
+    algo = 8.0 * N * rows + 4.0 * rows + 8.0 * nnz
+    achieved = algo / (ms / 1e3) / 1e9
+    del y1, y2, alive
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"layer_kernel_{args.workload}.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    props = torch.cuda.get_device_properties(d_in.device)
+    sms = props.multi_processor_count
+    smem_gbs = 128.0 * sms * (sm_mhz or 0) * 1e6 / 1e9 if sm_mhz else None
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+            "kernel": f"sdnn::layer_kernel (layer 1 of the workload, {rows} rows)",
+            "per": "one launch", "algorithmic_bytes_per_launch": algo, "avg_launch_ms": ms,
+            "frac_of_8tbs": achieved / 8000.0,
+            "smem_gather_bytes_per_launch": 4.0 * 32 * N * rows,
+            "smem_peak_gbs": smem_gbs, "sms": sms, "sm_mhz": sm_mhz}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -222,27 +310,27 @@ def run_ours(args):
     N, L, B, bias, t_default = WORKLOADS[args.workload]
     threshold = args.threshold if args.threshold is not None else t_default
     edges = float(B) * NNZ * N * L
-    # each rank runs its own batch (weak scaling over independent samples);
-    # the rows are generated on the device (bitwise equal to the host generator)
-    d_in = torch.empty((B, N), dtype=torch.float32, device=dev)
-    sg.generate_inputs_device(N, SEED, rank * B, B, d_in.data_ptr())
+    # the twelve uneven batches use the first rows of the same seeded stream,
+    # the timed batch the first B of them (each rank its own rows: weak scaling)
+    sizes = uneven_sizes() if not args.no_uneven else np.zeros(0, np.int64)
+    total_uneven = int(sizes.sum())
+    rows_all = max(B, total_uneven)
+    d_all = torch.empty((rows_all, N), dtype=torch.float32, device=dev)
+    sg.generate_inputs_device(N, SEED, rank * rows_all, rows_all, d_all.data_ptr())
+    d_in = d_all[:B]
     d_flags = torch.zeros(B, dtype=torch.int32, device=dev)
     torch.cuda.synchronize()
 
-    eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=B, bias=bias,
+    eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=rows_all, bias=bias,
                     num_centroids=args.centroids, device=local, tile_rows=args.tile,
                     threads=args.threads, merge_start=args.merge_start,
                     merge_every=args.merge_every)
     t0 = time.perf_counter()
     weights = load_weights(eng, args, N, L)
     pack_s = time.perf_counter() - t0
-    if not args.no_autotune and not args.tile:
-        rec = os.path.join(args.record_dir, f"autotune_{args.workload}.jsonl")
-        os.makedirs(os.path.dirname(rec), exist_ok=True)
-        if os.path.exists(rec):
-            os.remove(rec)
-        rows = args.tune_rows or B
-        eng.autotune_device(d_in.data_ptr(), rows, rec)
+    t0 = time.perf_counter()
+    record = autotune(eng, args, args.workload, d_in.data_ptr(), args.tune_rows or B)
+    tune_s = time.perf_counter() - t0
 
     # a real (non-default) stream: the engine orders its own stream after it and
     # makes it wait for the engine, so events recorded here bracket the work
@@ -256,28 +344,14 @@ def run_ours(args):
         step()
     torch.cuda.synchronize()
     flags_ref = d_flags.cpu().numpy().copy()
-
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    per_step = []
     with Clocks(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            s0 = torch.cuda.Event(enable_timing=True)
-            s1 = torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            step()
-            s1.record(stream)
-            per_step.append((s0, s1))
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    elapsed_ms = ev0.elapsed_time(ev1)
+        elapsed_ms, step_ms = time_steps(torch, stream, step, args.steps)
+    clocks = clk.summary()
     if dist:
         dist.barrier()
     st = eng.stats()  # stage events of the last step
-    step_ms = [a.elapsed_time(b) for a, b in per_step]
     flags = d_flags.cpu().numpy()
     assert np.array_equal(flags, flags_ref), "category set changed between steps"
     t = torch.tensor([elapsed_ms], dtype=torch.float64)
@@ -288,60 +362,46 @@ def run_ours(args):
     value = world * edges * args.steps / (max_ms / 1e3)
     ms_per_step = max_ms / args.steps
 
-    # roofline of the dominant kernel: the plain layer kernel of the pre-threshold stage
+    peak, peak_kind = peaks()
+    # the pre-threshold stage as a whole (binary layer 0, layer kernels, merge steps)
     nnz_layer = st["weight_nnz"] / L
     T = st["threshold"]
     pre_bytes = 8.0 * N * st["pre_row_layers"] + 4.0 * st["pre_row_layers"] + 8.0 * nnz_layer * T
     pre_s = st["stage_ms"][0] / 1e3
-    peak, peak_kind = peaks()
-    achieved = pre_bytes / pre_s / 1e9 if pre_s > 0 else 0.0
-    # DRAM bytes per plain layer from the committed ncu launch list of this workload
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", f"layer_kernel_{args.workload}.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
-    launches_pre = max(1, T)
-    # shared-memory ceiling of the gather (32 operands of 4 B per wavefront, one
-    # wavefront per SM clock): the roof that binds this kernel
-    sm_clk = 2.07e9
-    smem_gbs = 128.0 * 152 * sm_clk / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "kernel": "sdnn::layer_kernel + layer0_bits_kernel (plain layers below the threshold)",
-                "peak_kind": peak_kind, "per": "plain layer (one launch per layer)",
-                "algorithmic_bytes_per_launch": pre_bytes / launches_pre,
-                "avg_launch_ms": st["stage_ms"][0] / launches_pre,
-                "frac_of_8tbs": achieved / 8000.0,
-                "smem_gather_bytes_per_launch": 4.0 * 32 * N * st["pre_row_layers"] / launches_pre,
-                "smem_peak_gbs": smem_gbs}
+    pre_stage = {"bytes": pre_bytes, "ms": st["stage_ms"][0],
+                 "achieved_gbs": pre_bytes / pre_s / 1e9 if pre_s > 0 else 0.0,
+                 "frac": (pre_bytes / pre_s / 1e9) / peak if pre_s > 0 else 0.0,
+                 "layers": T, "row_layers": st["pre_row_layers"]}
+    roofline = layer_kernel_roofline(torch, sg, eng, d_in, B, N, stream, peak, peak_kind,
+                                     clocks.get("sm_mhz"), args)
 
     # end to end through the public host API: pinned host inputs in, survivor ids out
     host_t = torch.empty((B, N), dtype=torch.float32, pin_memory=True)
     host_t.copy_(d_in)
     host = host_t.numpy()
+    n_e2e = max(1, min(args.steps, args.e2e_steps))
 
-    def time_host_calls():
-        eng.infer(host, want_flags=False, want_ids=True)
+    def time_host_calls(fn):
+        fn()
         times, n = [], 0
-        for _ in range(max(1, min(args.steps, 10))):
+        for _ in range(n_e2e):
             t0 = time.perf_counter()
-            _, ids = eng.infer(host, want_flags=False, want_ids=True)
+            _, ids = fn()
             times.append(time.perf_counter() - t0)
             n = len(ids)
         return statistics.median(times), n
 
     # streamed ingest (the default): the rows copy in pieces and the layers
     # before the first merge run on each piece while the next ones copy
-    e2e_s, count = time_host_calls()
+    e2e_s, count = time_host_calls(lambda: eng.infer(host, want_flags=False, want_ids=True))
     pieces = eng.stats()["input_pieces"]
     assert count == int(flags.sum())
     e2e = {"value": world * edges / e2e_s, "unit": "edges/s", "h2d_bytes_per_step": B * N * 4,
            "d2h_bytes_per_step": 4 + 4 * count, "ms_per_step": e2e_s * 1e3,
-           "input_pieces": pieces}
+           "input_pieces": pieces, "api": "sdnn_infer_host (FP32 host rows)"}
     # the same call with one copy of the whole batch before the first layer
     eng.set_input_streaming(-1)
-    one_s, count1 = time_host_calls()
+    one_s, count1 = time_host_calls(lambda: eng.infer(host, want_flags=False, want_ids=True))
     eng.set_input_streaming(0)
     assert count1 == count
     e2e_one_copy = {"value": world * edges / one_s, "unit": "edges/s",
@@ -350,35 +410,58 @@ def run_ours(args):
     # the same with the inputs as one-bit host rows (the inputs are 0/1): 32x fewer bytes
     bits_t = torch.from_numpy(sg.pack_bits(host)).pin_memory()
     bits = bits_t.numpy()
-    eng.infer_bits(bits, want_flags=False, want_ids=True)
-    e2b_t = []
-    for _ in range(max(1, min(args.steps, 10))):
-        t0 = time.perf_counter()
-        _, ids_b = eng.infer_bits(bits, want_flags=False, want_ids=True)
-        e2b_t.append(time.perf_counter() - t0)
-    assert len(ids_b) == count
-    e2b_s = statistics.median(e2b_t)
+    e2b_s, count_b = time_host_calls(lambda: eng.infer_bits(bits, want_flags=False, want_ids=True))
+    assert count_b == count
     e2e_bits = {"value": world * edges / e2b_s, "unit": "edges/s",
                 "h2d_bytes_per_step": int(bits.nbytes), "d2h_bytes_per_step": 4 + 4 * count,
                 "ms_per_step": e2b_s * 1e3, "api": "sdnn_infer_host_bits"}
     del host_t, host, bits_t, bits
 
+    # uneven batches in one launch schedule against the same batches one by one
+    uneven = None
+    if total_uneven:
+        offs = np.concatenate([[0], np.cumsum(sizes)])
+        u_flags = torch.zeros(total_uneven, dtype=torch.int32, device=dev)
+        ptrs = [d_all[int(offs[i])].data_ptr() for i in range(len(sizes))]
+        fptrs = [u_flags[int(offs[i]):].data_ptr() for i in range(len(sizes))]
+        res = {}
+        for name, fn in (("one_schedule", lambda: eng.infer_batches_device(ptrs, sizes, fptrs, stream.cuda_stream)),
+                         ("one_by_one", lambda: [eng.infer_device(p, int(n), f, stream.cuda_stream)
+                                                 for p, n, f in zip(ptrs, sizes, fptrs)])):
+            for _ in range(2):
+                fn()
+            ms, _ = time_steps(torch, stream, fn, max(1, min(args.steps, 5)))
+            res[name] = (ms / max(1, min(args.steps, 5)), u_flags.cpu().numpy().copy())
+        u_edges = float(total_uneven) * NNZ * N * L
+        uneven = {"batches": sizes.tolist(), "rows": total_uneven,
+                  "one_schedule_ms": res["one_schedule"][0], "one_by_one_ms": res["one_by_one"][0],
+                  "edges_per_s": u_edges / (res["one_schedule"][0] / 1e3),
+                  "speedup_vs_one_by_one": res["one_by_one"][0] / res["one_schedule"][0],
+                  "category_sets_equal": bool(np.array_equal(res["one_schedule"][1],
+                                                             res["one_by_one"][1])),
+                  "survivors": int(res["one_schedule"][1].sum())}
+        del u_flags
+
     # plain per-layer path (SNIG mode) on the same batch and the same resident weights
     eng.set_mode("SNIG", L)
     plain_flags = torch.zeros(B, dtype=torch.int32, device=dev)
-    for _ in range(2):
-        eng.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
-    torch.cuda.synchronize()
-    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    eng.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
     psteps = max(1, min(args.steps, 3))
-    p0.record(stream)
-    for _ in range(psteps):
-        eng.infer_device(d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream)
-    p1.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = p0.elapsed_time(p1) / psteps
+    p_ms, _ = time_steps(torch, stream, lambda: eng.infer_device(
+        d_in.data_ptr(), B, plain_flags.data_ptr(), stream.cuda_stream), psteps)
+    plain_ms = p_ms / psteps
     pst = eng.stats()
     plain_exact = bool(np.array_equal(plain_flags.cpu().numpy(), flags))
+    launches = st["launches"] * args.steps
+    eng.close()
+    del d_all, d_in, plain_flags
+    torch.cuda.empty_cache()
+
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        for wl in args.extra_workloads.split(","):
+            if wl and wl != args.workload:
+                extra[wl] = run_extra(args, sg, torch, wl, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -406,20 +489,60 @@ def run_ours(args):
             "p99_ms": sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))],
             "survivors": int(flags.sum()),
             "stage_ms": st["stage_ms"],
-            "pack_s": pack_s, "weights": weights,
+            "pack_s": pack_s, "weights": weights, "autotune_s": tune_s,
+            "autotune_record": os.path.relpath(record, ROOT) if record else None,
             "plain": {"ms_per_inference": plain_ms, "edges_per_s": edges / (plain_ms / 1e3),
                       "category_set_equal": plain_exact, "row_layers": pst["row_layers"]},
             "speedup_vs_plain": plain_ms / ms_per_step,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "e2e_one_copy": e2e_one_copy, "e2e_bit_inputs": e2e_bits,
-            "gpu_launches": st["launches"] * args.steps,
-            "clocks": clk.summary(),
+            "roofline": roofline, "pre_stage": pre_stage, "cpu_baseline": cpu, "e2e": e2e,
+            "e2e_one_copy": e2e_one_copy, "e2e_bit_inputs": e2e_bits,
+            "uneven": uneven,
+            "gpu_launches": launches,
+            "clocks": clocks,
         }
+        line.update(extra)
         if not args.no_serve:
             line["serving"] = run_serving(args, sg, local)
         print(json.dumps(line), flush=True)
-    eng.close()
     if dist:
         dist.destroy_process_group()
+
+
+def run_extra(args, sg, torch, workload, local):
+    """Another SDGC workload on the same GPU, reported as an extra key: SNICIT
+    (autotuned) and the plain path, device-resident inputs."""
+    import numpy as np
+    N, L, B, bias, t_default = WORKLOADS[workload]
+    dev = f"cuda:{local}"
+    d_in = torch.empty((B, N), dtype=torch.float32, device=dev)
+    sg.generate_inputs_device(N, SEED, 0, B, d_in.data_ptr())
+    d_flags = torch.zeros(B, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    with sg.Engine(N, L, mode="SNICIT", threshold=t_default, batch=B, bias=bias,
+                   num_centroids=args.centroids, device=local) as eng:
+        eng.generate_weights(SEED, NNZ, 0.0625)
+        eng.finalize()
+        autotune(eng, args, workload, d_in.data_ptr(), B)
+        fn = lambda: eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr(), stream.cuda_stream)
+        for _ in range(args.warmup):
+            fn()
+        ms, per = time_steps(torch, stream, fn, args.steps)
+        st = eng.stats()
+        flags = d_flags.cpu().numpy().copy()
+        eng.set_mode("SNIG", L)
+        fn()
+        pms, _ = time_steps(torch, stream, fn, 3)
+        plain = d_flags.cpu().numpy()
+    edges = float(B) * NNZ * N * L
+    del d_in, d_flags
+    torch.cuda.empty_cache()
+    return {"workload": workload, "ms_per_inference": ms / args.steps,
+            "edges_per_s": edges / (ms / args.steps / 1e3), "p50_ms": statistics.median(per),
+            "plain_ms": pms / 3, "speedup_vs_plain": (pms / 3) / (ms / args.steps),
+            "category_set_equal": bool(np.array_equal(flags, plain)),
+            "survivors": int(flags.sum()), "stage_ms": st["stage_ms"],
+            "threshold": st["threshold"], "tile_rows": st["tile_rows"],
+            "threads": st["threads"], "merge_start": st["merge_start"]}
 
 
 UNEVEN = {
@@ -589,6 +712,9 @@ CASES = {
     "plain-n65536": (65536, 3, 2048, "SNIG", 3),
     "plain-n4096-30k": (4096, 3, 30000, "SNIG", 3),
     "chain-n65536": (65536, 40, 2048, "SNICIT", 30),
+    "plain-n65536-4k": (65536, 3, 4096, "SNIG", 3),
+    "plain-n16384": (16384, 3, 16384, "SNIG", 3),
+    "residue-n16384": (16384, 24, 4096, "SNICIT", 6),
 }
 
 
@@ -599,7 +725,8 @@ def run_case(args):
     Y0 = sg.generate_inputs(N, SEED, 0, B)
     eng = sg.Engine(N, L, mode=mode, threshold=t, batch=B, bias=sg.load().sdnn_reference_bias(N),
                     num_centroids=args.centroids, tile_rows=args.tile, threads=args.threads,
-                    merge_start=args.merge_start, merge_every=args.merge_every)
+                    merge_start=args.merge_start, merge_every=args.merge_every,
+                    merge=not args.case.startswith("residue"))
     eng.generate_weights(SEED, NNZ, 0.0625)
     for _ in range(2):
         eng.infer(Y0)
@@ -613,7 +740,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sdgc-4096x480", choices=sorted(WORKLOADS) + sorted(UNEVEN))
+    ap.add_argument("--workload", default="sdgc-65536x1920", choices=sorted(WORKLOADS) + sorted(UNEVEN))
     ap.add_argument("--threshold", type=int, default=None)
     ap.add_argument("--centroids", type=int, default=50)
     ap.add_argument("--tune-rows", type=int, default=0, help="rows used by the autotuner (0 = all)")
@@ -628,6 +755,13 @@ def main():
     ap.add_argument("--weights-cache", default=None,
                     help="directory of packed-weight files (written on the first run)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true",
+                    help="skip the twelve uneven batches (one schedule vs one by one)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the extra workloads")
+    ap.add_argument("--extra-workloads", default="sdgc-4096x480",
+                    help="comma-separated workloads reported as extra keys")
+    ap.add_argument("--e2e-steps", type=int, default=5,
+                    help="host-API calls timed per end-to-end form (median)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serve-only", action="store_true", help="only the serving-loop measurement")

@@ -118,9 +118,16 @@ int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
   if (cfg0.mode == SDNN_MODE_SNICIT) {
     Trial bs = best;
     bs.ms = 1e30f;
-    for (int th : {30, 60, 120, 240}) {
-      if (th >= cfg0.num_layers) continue;
+    // thresholds {30, 60, 120, 240} x centroid counts {50, 100, 200}, and no
+    // clustering at all (threshold = L: the plain path with merging), so the
+    // chosen setting is never slower than plain on the sample
+    std::vector<int> ths;
+    for (int th : {30, 60, 120, 240})
+      if (th < cfg0.num_layers) ths.push_back(th);
+    ths.push_back(cfg0.num_layers);
+    for (int th : ths) {
       for (int k : {50, 100, 200}) {
+        if (th == cfg0.num_layers && k != 50) continue;  // no clustering: one trial
         sdnn::engine_set_snicit(e, th, k);
         Trial t{best.tile, best.threads, th, k, cfg0.merge_start, 0.f, 0, 0};
         t.status = time_setting(e, smp, -1, t.ms, t.survivors);

@@ -124,7 +124,7 @@ struct sdnn_engine {
 
   // device buffers
   int64_t cap = 0;
-  int Kmax = 0;
+  int Kcap = 0;  // rows of the centroid buffers
   float* d_y[2] = {nullptr, nullptr};
   int32_t* d_list[2] = {nullptr, nullptr};
   int32_t* d_rlist[2] = {nullptr, nullptr};
@@ -398,8 +398,10 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   drop_graph(e);
   const int64_t cap = std::max<int64_t>(rows, e->cfg.batch);
   const size_t N = (size_t)e->N;
-  const int K = std::max(1, e->cfg.num_centroids);
-  e->Kmax = K;
+  // centroid buffers sized for the autotuner's largest candidate count too,
+  // so switching counts needs no reallocation
+  const int K = std::max(std::max(1, e->cfg.num_centroids), 200);
+  e->Kcap = K;
   auto A = [&](auto** p, size_t bytes) -> cudaError_t {
     return cudaMalloc((void**)p, std::max<size_t>(bytes, 16));
   };
@@ -975,7 +977,7 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
     c.live = live;
     c.live_count = live_count;
     c.N = e->N;
-    c.K = e->Kmax;
+    c.K = std::max(1, e->cfg.num_centroids);
     c.seed = e->cfg.seed;
     c.cand = e->d_cand;
     c.ncand = e->d_ncand;
@@ -1090,7 +1092,7 @@ int run_phase(sdnn_engine* e, int slot, int phase, int64_t rows, const float* d_
   }
   const bool streamed = e->pipe_start > 0 && (phase == PH_ALL || phase == PH_PRE);
   GraphSlot& g = e->graphs[streamed ? 5 + slot : slot];
-  const GraphKey key{0, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
+  const GraphKey key{0, d_in, d_flags, effective_threshold(e), std::max(1, e->cfg.num_centroids), e->cfg.mode,
                      e->key.T, e->threads,
                      phase == PH_POST_CHAIN ? e->chain_kc * 4 + e->chain_kind : 0,
                      streamed ? e->pipe_start : 0};
@@ -1246,7 +1248,7 @@ int build_full_graph(sdnn_engine* e, FullGraph& fg, int64_t rows, const float* d
 int run_full(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
   const int slot = e->pipe_start > 0 ? 1 : 0;
   FullGraph& fg = e->full[slot];
-  const GraphKey key{0, d_in, d_flags, effective_threshold(e), e->Kmax, e->cfg.mode,
+  const GraphKey key{0, d_in, d_flags, effective_threshold(e), std::max(1, e->cfg.num_centroids), e->cfg.mode,
                      e->key.T, e->threads, 0, e->pipe_start};
   if (!fg.exec || !(fg.key == key)) {
     if (fg.exec) cudaGraphExecDestroy(fg.exec);
@@ -2102,7 +2104,7 @@ void engine_set_snicit(sdnn_engine* e, int threshold, int centroids) {
   e->cfg.threshold = threshold;
   if (centroids != e->cfg.num_centroids) {
     e->cfg.num_centroids = centroids;
-    free_buffers(e);
+    if (centroids > e->Kcap) free_buffers(e);  // the centroid buffers hold Kcap rows
   }
   drop_graph(e);
 }
