@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SDNN_ABI_VERSION 2
+#define SDNN_ABI_VERSION 3
 
 /* Status codes returned by every entry point. */
 typedef enum sdnn_status {
@@ -102,6 +102,9 @@ typedef struct sdnn_config {
                                            /* per-layer launches where it cannot run)     */
 #define SDNN_FLAG_NO_STREAMED_INPUT 64     /* host FP32 inputs: one copy of the whole batch */
                                            /* before the first layer (no piecewise ingest) */
+#define SDNN_FLAG_DENSE_RESIDUE 256        /* SNICIT: every residue row stays a dense row    */
+                                           /* (no sparse residue lists; categories identical,*/
+                                           /* activations within FP32 rounding)            */
 #define SDNN_FLAG_HOST_POST_CHOICE 128     /* SNICIT: the host reads back what the          */
                                            /* clustering left and picks the post-threshold  */
                                            /* path (a host sync mid-inference) instead of   */
@@ -136,7 +139,9 @@ typedef struct sdnn_stats {
                             memory), 4 grid-wide chain kernel                     */
   int32_t device_post_choice; /* SNICIT: 1 when the post-threshold path was chosen on
                             the device (the whole inference one graph launch)     */
-  int32_t reserved1;
+  int32_t sparse_residue_rows; /* SNICIT: residue rows at the threshold kept as sparse
+                            (position, value) lists (<= N/8 nonzeros)             */
+  int64_t sparse_row_layers;   /* sparse residue rows summed over the post layers   */
 } sdnn_stats;
 
 typedef struct sdnn_engine sdnn_engine;

@@ -18,6 +18,7 @@ FLAG_NO_CHAIN_STREAM = 16
 FLAG_NO_GRID_CHAIN = 32
 FLAG_NO_STREAMED_INPUT = 64
 FLAG_HOST_POST_CHOICE = 128
+FLAG_DENSE_RESIDUE = 256
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "I/O error",
@@ -57,7 +58,7 @@ class Stats(ctypes.Structure):
         ("weight_nnz", ctypes.c_int64), ("centroid_candidates", ctypes.c_int32),
         ("merge_start", ctypes.c_int32), ("merge_every", ctypes.c_int32),
         ("post_kernel", ctypes.c_int32), ("device_post_choice", ctypes.c_int32),
-        ("reserved1", ctypes.c_int32),
+        ("sparse_residue_rows", ctypes.c_int32), ("sparse_row_layers", ctypes.c_int64),
     ]
 
 

@@ -27,7 +27,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 SOURCES = [
     "layer_q1024.cu", "layer_q4096.cu", "layer_q16384.cu", "layer_generic.cu",
     "layer_dispatch.cu", "layer0_bits.cu", "post_chain.cu", "post_grid.cu", "aux.cu", "engine.cpp", "wpack.cpp", "packfile.cpp", "inputs_bin.cpp", "tsv.cpp", "gen.cpp",
-    "autotune.cpp", "serve.cpp", "dedup.cu", "gen_device.cu", "selftest.cu", "noalloc.cu",
+    "autotune.cpp", "serve.cpp", "dedup.cu", "gen_device.cu", "selftest.cu", "noalloc.cu", "residue_sparse.cu",
 ]
 
 

@@ -27,7 +27,7 @@ __global__ void set_scalar_kernel(int32_t* p, int32_t v) { *p = v; }
 void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s) { set_scalar_kernel<<<1, 1, 0, s>>>(p, v); }
 
 __global__ void post_choice_kernel(const PostChoiceArgs a, cudaGraphConditionalHandle h) {
-  const int residues = *a.rcount, centroids = *a.ccount;
+  const int residues = *a.rcount + (a.scount ? *a.scount : 0), centroids = *a.ccount;
   int body = 0;
   if (!a.no_chain && residues == 0 && centroids >= 1) {
     int i = 0, kc = 1;

@@ -39,6 +39,11 @@ struct DevLayer {
   int32_t* grp = nullptr;
   float* bias = nullptr;
   float* sums = nullptr;  // layer 0 with one common value: w added k times, k < 128
+  // transposed layer for the sparse residue update: out-edges of every input
+  // position (output positions, values unless the layer has one value)
+  int32_t* tr_off = nullptr;
+  uint16_t* tr_out = nullptr;
+  float* tr_val = nullptr;
   bool constw = true;
   float wconst = 0.f;
   int64_t nnz = 0;
@@ -184,6 +189,19 @@ struct sdnn_engine {
   int32_t* d_fbcount2 = nullptr;
   int32_t* d_pcounts = nullptr;  // [kMaxPieces][L + 2]
   int32_t* d_plist[2] = {nullptr, nullptr};  // [cap] row lists of the pieces' layers
+  // sparse residue rows (SNICIT post layers, whole-row layouts): per post layer
+  // p the dense residue rows are d_rlist[p & 1] and the sparse ones
+  // d_slist[p & 1] with their entries in d_sp*[p & 1]; d_rtmp collects the
+  // non-empty rows of a dense residue launch before they are split
+  bool sparse_res = false;
+  int32_t sp_cap = 0;  // entries per sparse row (N / 8)
+  int32_t* d_sp_idx[2] = {nullptr, nullptr};
+  float* d_sp_val[2] = {nullptr, nullptr};
+  int32_t* d_sp_cnt[2] = {nullptr, nullptr};
+  int32_t* d_slist[2] = {nullptr, nullptr};
+  int32_t* d_scounts = nullptr;  // [L + 4]
+  int32_t* d_rtmp = nullptr;
+  int32_t* d_tcounts = nullptr;  // [L + 4]
   int pipe_start = 0;            // first layer of the graphed part (0: every layer)
   int last_pieces = 0;
 
@@ -252,6 +270,9 @@ void free_weights(sdnn_engine* e) {
     dfree(d.grp);
     dfree(d.bias);
     dfree(d.sums);
+    dfree(d.tr_off);
+    dfree(d.tr_out);
+    dfree(d.tr_val);
   }
   e->dl.clear();
 }
@@ -305,6 +326,15 @@ void free_buffers(sdnn_engine* e) {
   dfree(e->d_ticket2);
   dfree(e->d_fallback2);
   dfree(e->d_fbcount2);
+  for (int i = 0; i < 2; ++i) {
+    dfree(e->d_sp_idx[i]);
+    dfree(e->d_sp_val[i]);
+    dfree(e->d_sp_cnt[i]);
+    dfree(e->d_slist[i]);
+  }
+  dfree(e->d_scounts);
+  dfree(e->d_rtmp);
+  dfree(e->d_tcounts);
   if (e->h_counts) cudaFreeHost(e->h_counts);
   e->h_counts = nullptr;
   e->cap = 0;
@@ -340,6 +370,9 @@ void choose_layout(sdnn_engine* e) {
   e->Q = N > 32768 ? 16384 : N;
   e->nq = N / e->Q;
   e->G = N / 32;
+  // sparse residue rows need the whole row of one warp in shared memory
+  e->sparse_res = e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_DENSE_RESIDUE) &&
+                  sparse_residue_warps(N) > 0;
 }
 
 int choose_kernel(sdnn_engine* e) {
@@ -435,6 +468,18 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_ids, (size_t)cap * 4));
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
+  if (e->sparse_res) {
+    e->sp_cap = std::max(1, e->N / 8);
+    for (int i = 0; i < 2; ++i) {
+      T(A(&e->d_sp_idx[i], (size_t)cap * e->sp_cap * 4));
+      T(A(&e->d_sp_val[i], (size_t)cap * e->sp_cap * 4));
+      T(A(&e->d_sp_cnt[i], (size_t)cap * 4));
+      T(A(&e->d_slist[i], (size_t)cap * 4));
+    }
+    T(A(&e->d_scounts, (size_t)(e->L + 4) * 4));
+    T(A(&e->d_rtmp, (size_t)cap * 4));
+    T(A(&e->d_tcounts, (size_t)(e->L + 4) * 4));
+  }
   // grid chain rows: a fresh buffer per layer (wide layouts only, where it runs)
   if (e->N >= 16384) T(A(&e->d_gscratch, grid_chain_scratch_floats(e->L, e->nq, e->Q) * 4));
   T(A(&e->d_gbar, 16));
@@ -607,6 +652,50 @@ int upload_layer(sdnn_engine* e, int l, const PackedView& p, std::string& err) {
     }
     T(cudaMalloc((void**)&d.sums, sizeof(sums)));
     if (rc == cudaSuccess) T(cudaMemcpy(d.sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
+  }
+  if (rc == cudaSuccess && e->sparse_res && e->nq == 1) {
+    // out-edges of every input position, from the packed slots (padding slots
+    // point past the chunk and are skipped), each input's edges by output
+    const int32_t scale = slot_index_in_bytes(e->Q) ? 4 : 1;
+    const int32_t N = e->N, Q = e->Q;
+    std::vector<int32_t> off(N + 1, 0);
+    for (int32_t g = 0; g < e->G; ++g)
+      for (int32_t b = p.grp_blk[g]; b < p.grp_blk[g + 1]; ++b)
+        for (int k = 0; k < 128; ++k) {
+          const int32_t j = p.idx[(size_t)b * 128 + k] / scale;
+          if (j < Q) off[j + 1]++;
+        }
+    for (int32_t j = 0; j < N; ++j) off[j + 1] += off[j];
+    const size_t ne = (size_t)off[N];
+    std::vector<std::pair<uint16_t, float>> edges(ne);
+    std::vector<int32_t> fill(off.begin(), off.end() - 1);
+    for (int32_t g = 0; g < e->G; ++g)
+      for (int32_t b = p.grp_blk[g]; b < p.grp_blk[g + 1]; ++b)
+        for (int k = 0; k < 128; ++k) {
+          const int32_t j = p.idx[(size_t)b * 128 + k] / scale;
+          if (j >= Q) continue;
+          const float w = p.constw ? p.wconst : p.val[(size_t)b * 128 + k];
+          edges[fill[j]++] = {(uint16_t)(32 * g + (k >> 2)), w};
+        }
+    std::vector<uint16_t> tout(ne);
+    std::vector<float> tval(p.constw ? 0 : ne);
+    for (int32_t j = 0; j < N; ++j) {
+      std::sort(edges.begin() + off[j], edges.begin() + off[j + 1],
+                [](const std::pair<uint16_t, float>& x, const std::pair<uint16_t, float>& y) {
+                  return x.first < y.first;
+                });
+      for (int32_t t = off[j]; t < off[j + 1]; ++t) {
+        tout[t] = edges[t].first;
+        if (!p.constw) tval[t] = edges[t].second;
+      }
+    }
+    T(cudaMalloc((void**)&d.tr_off, (size_t)(N + 1) * 4));
+    T(cudaMalloc((void**)&d.tr_out, std::max<size_t>(ne * 2, 16)));
+    if (!p.constw) T(cudaMalloc((void**)&d.tr_val, std::max<size_t>(ne * 4, 16)));
+    if (rc == cudaSuccess) T(cudaMemcpy(d.tr_off, off.data(), (size_t)(N + 1) * 4, cudaMemcpyHostToDevice));
+    if (rc == cudaSuccess && ne) T(cudaMemcpy(d.tr_out, tout.data(), ne * 2, cudaMemcpyHostToDevice));
+    if (rc == cudaSuccess && d.tr_val && ne)
+      T(cudaMemcpy(d.tr_val, tval.data(), ne * 4, cudaMemcpyHostToDevice));
   }
   e->dl[l] = d;
   if (rc != cudaSuccess) {
@@ -942,6 +1031,10 @@ int enqueue_piece(sdnn_engine* e, int p, int64_t r0, int64_t n, int m, const flo
   return SDNN_OK;
 }
 
+SparseRows sparse_rows(const sdnn_engine* e, int b) {
+  return SparseRows{e->d_sp_idx[b], e->d_sp_val[b], e->d_sp_cnt[b], e->sp_cap};
+}
+
 // Enqueues one phase of an inference of `rows` rows read from d_in.
 int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t* d_flags,
             bool capturing) {
@@ -968,6 +1061,10 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
       e->launches++;
     }
     CK(cudaMemsetAsync(e->d_rcounts, 0, (size_t)(L + 4) * 4, s));
+    if (e->sparse_res) {
+      CK(cudaMemsetAsync(e->d_scounts, 0, (size_t)(L + 4) * 4, s));
+      CK(cudaMemsetAsync(e->d_tcounts, 0, (size_t)(L + 4) * 4, s));
+    }
     launch_zero_rows(e->d_rows, e->d_iscent, e->d_resflag, s);
     e->launches++;
     CK(cudaMemsetAsync(e->d_ccount, 0, 16, s));
@@ -985,12 +1082,19 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
     c.clist = e->d_clist;
     c.ccount = e->d_ccount;
     c.cslot = e->d_cslot;
-    c.rlist = e->d_rlist[0];
-    c.rcount = e->d_rcounts;
+    // residue rows of the clustering: straight to the dense list, or first to
+    // d_rtmp to be split into dense and sparse rows
+    c.rlist = e->sparse_res ? e->d_rtmp : e->d_rlist[0];
+    c.rcount = e->sparse_res ? e->d_tcounts : e->d_rcounts;
     c.is_centroid = e->d_iscent;
     c.err = e->d_err;
     launch_cluster(c, e->num_sms, s);
     e->launches += 4;
+    if (e->sparse_res) {
+      launch_split_residue(ybuf, e->d_rtmp, e->d_tcounts, sparse_rows(e, 0), e->d_rlist[0],
+                           e->d_rcounts, e->d_slist[0], e->d_scounts, e->N, e->num_sms, s);
+      e->launches++;
+    }
     if ((rc = record(e, 2, capturing))) return rc;
   }
   if (phase == PH_POST_LAYERS) {
@@ -1001,9 +1105,42 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
       if ((rc = layer_launch(e, l, EPI_CENTROID, in, out, e->d_clist, e->d_ccount, nullptr,
                              nullptr)))
         return rc;
+      if (!e->sparse_res) {
+        if ((rc = layer_launch(e, l, EPI_RESIDUE, in, out, e->d_rlist[p & 1], e->d_rcounts + p,
+                               e->d_rlist[(p + 1) & 1], e->d_rcounts + p + 1)))
+          return rc;
+        continue;
+      }
+      // dense residue rows: the layer kernel, then their split by nonzeros
       if ((rc = layer_launch(e, l, EPI_RESIDUE, in, out, e->d_rlist[p & 1], e->d_rcounts + p,
-                             e->d_rlist[(p + 1) & 1], e->d_rcounts + p + 1)))
+                             e->d_rtmp, e->d_tcounts + p + 1)))
         return rc;
+      const SparseRows next = sparse_rows(e, (p + 1) & 1);
+      launch_split_residue(out, e->d_rtmp, e->d_tcounts + p + 1, next, e->d_rlist[(p + 1) & 1],
+                           e->d_rcounts + p + 1, e->d_slist[(p + 1) & 1], e->d_scounts + p + 1,
+                           e->N, e->num_sms, s);
+      // sparse residue rows: scattered along the transposed layer
+      const DevLayer& d = e->dl[l];
+      SparseResArgs sa{};
+      sa.list_in = e->d_slist[p & 1];
+      sa.count_in = e->d_scounts + p;
+      sa.in = sparse_rows(e, p & 1);
+      sa.out = next;
+      sa.y_out = out;
+      sa.dense_list = e->d_rlist[(p + 1) & 1];
+      sa.dense_count = e->d_rcounts + p + 1;
+      sa.sparse_list = e->d_slist[(p + 1) & 1];
+      sa.sparse_count = e->d_scounts + p + 1;
+      sa.tr_off = d.tr_off;
+      sa.tr_out = d.tr_out;
+      sa.tr_val = d.tr_val;
+      sa.wconst = d.wconst;
+      sa.pre = e->d_pre;
+      sa.cslot = e->d_cslot;
+      sa.N = e->N;
+      sa.clampv = e->cfg.clamp;
+      CK(launch_sparse_residue(sa, e->num_sms, s));
+      e->launches += 2;
     }
     if ((rc = record(e, 3, capturing))) return rc;
   }
@@ -1050,6 +1187,14 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
   if (phase == PH_FINISH) {
     const int pf = L - T;
     launch_mark_rows(e->d_rlist[pf & 1], e->d_rcounts + pf, e->d_resflag, 1, s);
+    if (e->sparse_res) {
+      // the last sparse rows, written densely into the final buffer: from here
+      // on every residue row reads the same way
+      launch_densify(e->d_slist[pf & 1], e->d_scounts + pf, sparse_rows(e, pf & 1),
+                     e->d_y[(L - 1) & 1], e->N, e->num_sms, s);
+      launch_mark_rows(e->d_slist[pf & 1], e->d_scounts + pf, e->d_resflag, 1, s);
+      e->launches += 2;
+    }
     launch_recover(e->d_y[(L - 1) & 1], live, live_count, e->d_cslot, e->d_clist, e->d_iscent,
                    e->d_resflag, e->N, d_flags, s);
     launch_mark_rows(live, live_count, e->d_state, 2, s);
@@ -1148,6 +1293,7 @@ int build_full_graph(sdnn_engine* e, FullGraph& fg, int64_t rows, const float* d
 
   PostChoiceArgs pc{};
   pc.rcount = e->d_rcounts;
+  pc.scount = e->sparse_res ? e->d_scounts : nullptr;
   pc.ccount = e->d_ccount;
   pc.choice = e->d_choice;
   pc.chain_cap = e->chain_cap;
@@ -1297,8 +1443,11 @@ int run(sdnn_engine* e, int64_t rows, const float* d_in, int32_t* d_flags) {
     // what did the clustering leave?  (one small read-back per inference)
     CK(cudaMemcpyAsync(e->h_counts, e->d_rcounts, 4, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaMemcpyAsync(e->h_counts + 1, e->d_ccount, 4, cudaMemcpyDeviceToHost, e->stream));
+    e->h_counts[2] = 0;
+    if (e->sparse_res)
+      CK(cudaMemcpyAsync(e->h_counts + 2, e->d_scounts, 4, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
-    const int residues = e->h_counts[0], centroids = e->h_counts[1];
+    const int residues = e->h_counts[0] + e->h_counts[2], centroids = e->h_counts[1];
     // no residue left: one chain launch carries the centroid rows -- the
     // cluster kernel where the rows fit shared memory (measured faster: 1.6
     // and 7.2 us per layer at N = 4096 and 16384 against 13.8 and 11.8 for the
@@ -1360,6 +1509,7 @@ int prepare(sdnn_engine* e, int64_t rows) {
   }
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, true}, e->smem));
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
+  if (e->sparse_res) CK(sparse_residue_prepare(e->N));
   e->bits_chunked = e->nq > 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
                     layer0_bits_chunked_supported(e->N, e->Q);
   e->bits_grid = (e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
@@ -1403,9 +1553,18 @@ int collect_stats(sdnn_engine* e) {
   if (T < L) {
     CK(cudaMemcpy(rcounts.data(), e->d_rcounts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&ccount, e->d_ccount, 4, cudaMemcpyDeviceToHost));
-    for (int p = 0; p < L - T; ++p) post += ccount + rcounts[p];
+    std::vector<int32_t> scounts(L + 4, 0);
+    if (e->sparse_res)
+      CK(cudaMemcpy(scounts.data(), e->d_scounts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
+    int64_t sparse = 0;
+    for (int p = 0; p < L - T; ++p) {
+      post += ccount + rcounts[p] + scounts[p];
+      sparse += scounts[p];
+    }
     st.centroids = ccount;
-    st.residue_rows = rcounts[0];
+    st.residue_rows = rcounts[0] + scounts[0];
+    st.sparse_residue_rows = scounts[0];
+    st.sparse_row_layers = sparse;
     st.rows_out = 0;
   } else {
     st.rows_out = counts[L];
@@ -2068,7 +2227,10 @@ int sdnn_get_layer_rows(const sdnn_engine* ce, int64_t* out, int32_t num_layers)
   if (T < L) {
     CK(cudaMemcpy(rcounts.data(), e->d_rcounts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&ccount, e->d_ccount, 4, cudaMemcpyDeviceToHost));
-    for (int l = T; l < L; ++l) out[l] = (int64_t)ccount + rcounts[l - T];
+    std::vector<int32_t> scounts(L + 4, 0);
+    if (e->sparse_res)
+      CK(cudaMemcpy(scounts.data(), e->d_scounts, (size_t)(L + 4) * 4, cudaMemcpyDeviceToHost));
+    for (int l = T; l < L; ++l) out[l] = (int64_t)ccount + rcounts[l - T] + scounts[l - T];
   }
   return SDNN_OK;
 }

@@ -171,7 +171,8 @@ void launch_set_scalar(int32_t* p, int32_t v, cudaStream_t s);
 // (has_body 0) and never chosen.  The choice is also stored for the stats.
 constexpr int kPostBodies = 9;
 struct PostChoiceArgs {
-  const int32_t* rcount;  // residue rows at the threshold
+  const int32_t* rcount;  // residue rows at the threshold (dense)
+  const int32_t* scount;  // ... kept as sparse lists (nullptr: none)
   const int32_t* ccount;  // centroids kept
   int32_t* choice;        // out: the body taken
   int32_t chain_cap, grid_cap, no_chain;
@@ -263,5 +264,45 @@ void launch_dedup(const DedupArgs& a, int num_sms, cudaStream_t s);
 // alias[r] := root of r's chain, flags[r] := flags[root] for merged rows.
 void launch_resolve_alias(const int32_t* nrows, int32_t* alias, int32_t* flags, int32_t max_depth,
                           cudaStream_t s);
+
+
+// ---- sparse residue rows (residue_sparse.cu) ----
+// A residue row with at most `cap` nonzeros: entries [r * cap, r * cap + cnt[r])
+// of idx (positions, ascending) and val.
+struct SparseRows {
+  int32_t* idx;
+  float* val;
+  int32_t* cnt;
+  int32_t cap;
+};
+// One post-threshold layer over the sparse residue rows.
+struct SparseResArgs {
+  const int32_t* list_in;   // sparse rows of this layer
+  const int32_t* count_in;
+  SparseRows in, out;       // this layer's lists / the next layer's
+  float* y_out;             // rows that grow past `cap` are written here densely
+  int32_t* dense_list;      // ... and listed here (the next dense residue list)
+  int32_t* dense_count;
+  int32_t* sparse_list;     // the next sparse residue list
+  int32_t* sparse_count;
+  const int32_t* tr_off;    // transposed layer: out-edges of every input position
+  const uint16_t* tr_out;   // output positions
+  const float* tr_val;      // values, nullptr when the layer has one value
+  float wconst;
+  const float* pre;         // [K][N] centroid pre-activations of this layer (bias in)
+  const int32_t* cslot;     // row -> centroid slot
+  int32_t N;
+  float clampv;
+};
+size_t sparse_residue_smem_per_warp(int N);
+int sparse_residue_warps(int N);  // warps per CTA (0: rows too wide for shared memory)
+cudaError_t sparse_residue_prepare(int N);
+void launch_split_residue(const float* y, const int32_t* list, const int32_t* count,
+                          const SparseRows& out, int32_t* dense_list, int32_t* dense_count,
+                          int32_t* sparse_list, int32_t* sparse_count, int32_t N, int num_sms,
+                          cudaStream_t s);
+cudaError_t launch_sparse_residue(const SparseResArgs& a, int num_sms, cudaStream_t s);
+void launch_densify(const int32_t* list, const int32_t* count, const SparseRows& rows, float* y,
+                    int32_t N, int num_sms, cudaStream_t s);
 
 }  // namespace sdnn

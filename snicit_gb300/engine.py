@@ -24,7 +24,7 @@ class Engine:
                  device=0, tile_rows=0, threads=0, binary_first_layer=True, placement=True,
                  chain=True, merge=True, merge_start=0, merge_every=0, chain_stream=True,
                  grid_chain=True, streamed_input=True, input_piece_rows=0,
-                 device_post_choice=True, input_prefix_layers=0):
+                 device_post_choice=True, input_prefix_layers=0, sparse_residue=True):
         lib = load()
         cfg = Config()
         check(lib.sdnn_config_default(ctypes.byref(cfg)))
@@ -47,7 +47,8 @@ class Engine:
                 | (0 if chain_stream else _lib.FLAG_NO_CHAIN_STREAM)
                 | (0 if grid_chain else _lib.FLAG_NO_GRID_CHAIN)
                 | (0 if streamed_input else _lib.FLAG_NO_STREAMED_INPUT)
-                | (0 if device_post_choice else _lib.FLAG_HOST_POST_CHOICE))
+                | (0 if device_post_choice else _lib.FLAG_HOST_POST_CHOICE)
+                | (0 if sparse_residue else _lib.FLAG_DENSE_RESIDUE))
         cfg.merge_start = int(merge_start)
         cfg.merge_every = int(merge_every)
         cfg.input_piece_rows = int(input_piece_rows)
@@ -178,6 +179,8 @@ class Engine:
             "merge_start": s.merge_start, "merge_every": s.merge_every,
             "post_kernel": s.post_kernel, "input_pieces": s.input_pieces,
             "device_post_choice": s.device_post_choice,
+            "sparse_residue_rows": s.sparse_residue_rows,
+            "sparse_row_layers": s.sparse_row_layers,
         }
 
     def layer_rows(self):

@@ -43,7 +43,7 @@ def test_defaults_and_reference_bias():
     # main/SDGC.cu:49-54
     for n, b in ((65536, -0.45), (16384, -0.4), (4096, -0.35), (1024, -0.3), (77, 0.0)):
         assert lib.sdnn_reference_bias(n) == pytest.approx(b)
-    assert lib.sdnn_abi_version() == 2
+    assert lib.sdnn_abi_version() == 3
 
 
 def test_struct_layouts_match_the_c_abi():

@@ -644,3 +644,39 @@ def test_plain_path_is_bitwise_equal_to_slot_order_evaluation(tmp_path, N, L, B,
     assert np.array_equal(got_flags, alive.astype(np.int32))
     assert alive.sum() > 0
     assert np.array_equal(Y[alive].view(np.uint32), want[alive].view(np.uint32))
+
+
+@pytest.mark.parametrize("N,L,B,T,K", [(1024, 40, 600, 6, 16), (4096, 30, 200, 7, 32),
+                                       (256, 40, 500, 4, 8)])
+def test_sparse_residue_rows_match_dense_rows_and_oracle(N, L, B, T, K):
+    """Residue rows that keep few nonzeros become sparse (position, value)
+    lists after the threshold: the sparse update gives the dense update's
+    category set and agrees with the FP64 oracle within the FP32 bound; it is
+    bitwise repeatable.  Merging is off so that rows stay distinct and
+    residues persist past the threshold."""
+    seed = 4242 + N
+    bias = sg.load().sdnn_reference_bias(N)
+    Y0 = sg.generate_inputs(N, seed, 0, B)
+    out = {}
+    for sparse in (True, False):
+        with sg.Engine(N, L, mode="SNICIT", threshold=T, batch=B, bias=bias, num_centroids=K,
+                       merge=False, sparse_residue=sparse) as eng:
+            eng.generate_weights(seed)
+            flags, ids = eng.infer(Y0)
+            Y = eng.activations(B)
+            st = eng.stats()
+            flags2, _ = eng.infer(Y0)
+            Y2 = eng.activations(B)
+            assert np.array_equal(flags, flags2)
+            assert np.array_equal(Y.view(np.uint32), Y2.view(np.uint32))
+            out[sparse] = (flags, ids, Y, st)
+    st_s, st_d = out[True][3], out[False][3]
+    assert st_d["sparse_row_layers"] == 0
+    assert st_s["residue_rows"] > 0 and st_s["sparse_row_layers"] > 0, st_s
+    print(f"N={N} t={T}: {st_s['residue_rows']} residue rows at the threshold "
+          f"({st_s['sparse_residue_rows']} sparse), {st_s['sparse_row_layers']} sparse row-layers")
+    assert np.array_equal(out[True][0], out[False][0])
+    Yref, alive, Y32 = _ref(_layers(N, L, seed), N, bias, Y0)
+    for sparse in (True, False):
+        _check(out[sparse][2], out[sparse][0], out[sparse][1], Yref, alive,
+               f"sparse={sparse} N={N}", Y32=Y32)
