@@ -462,6 +462,8 @@ def run_ours(args):
         for wl in args.extra_workloads.split(","):
             if wl and wl != args.workload:
                 extra[wl] = run_extra(args, sg, torch, wl, local)
+        if not args.no_residue:
+            extra["residue_stage"] = run_residue(args, sg, torch, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -506,6 +508,98 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_residue(args, sg, torch, local, workload="sdgc-4096x480", threshold=6):
+    """A workload where residue rows persist past the threshold: the 4096 x 480
+    net clustered at layer 6 (rows not yet saturated) without merging, with
+    sparse residue lists and with dense residue rows only.  Reports the
+    post-threshold stage: time, residue row-layers (dense + sparse) and the
+    algorithmic bytes per second of the residue update."""
+    import numpy as np
+    N, L, B, bias, _ = WORKLOADS[workload]
+    dev = f"cuda:{local}"
+    d_in = torch.empty((B, N), dtype=torch.float32, device=dev)
+    sg.generate_inputs_device(N, SEED, 0, B, d_in.data_ptr())
+    d_flags = torch.zeros(B, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    out = {"workload": workload, "threshold": threshold, "merge": False}
+    flags = {}
+    for sparse in (True, False):
+        with sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=B, bias=bias,
+                       num_centroids=args.centroids, device=local, merge=False,
+                       sparse_residue=sparse) as eng:
+            eng.generate_weights(SEED, NNZ, 0.0625)
+            eng.finalize()
+            fn = lambda: eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr(), stream.cuda_stream)
+            for _ in range(2):
+                fn()
+            n = max(3, min(args.steps, 10))
+            ms, _ = time_steps(torch, stream, fn, n)
+            st = eng.stats()
+            flags[sparse] = d_flags.cpu().numpy().copy()
+            rl = eng.layer_rows()
+        post_ms = st["stage_ms"][2]
+        res_layers = int(st["post_row_layers"] - st["centroids"] * (L - threshold))
+        # per residue row-layer: read + write the row (8 N B) and the centroid
+        # pre-activations (4 N B) for dense rows; sparse rows count the same
+        # here (upper bound of what a dense update moves)
+        algo = 12.0 * N * res_layers + 8.0 * NNZ * N * (L - threshold)
+        out["sparse" if sparse else "dense"] = {
+            "ms_per_inference": ms / n, "post_stage_ms": post_ms,
+            "residue_rows_at_threshold": st["residue_rows"],
+            "sparse_rows_at_threshold": st["sparse_residue_rows"],
+            "residue_row_layers": res_layers, "sparse_row_layers": st["sparse_row_layers"],
+            "post_layers_with_residues": int(sum(1 for l in range(threshold, L)
+                                                 if rl[l] > st["centroids"])),
+            "post_dense_equivalent_gbs": algo / (post_ms / 1e3) / 1e9 if post_ms > 0 else None,
+            "survivors": int(flags[sparse].sum())}
+    out["category_sets_equal"] = bool(np.array_equal(flags[True], flags[False]))
+    out["post_speedup_sparse_vs_dense"] = (out["dense"]["post_stage_ms"] /
+                                           max(out["sparse"]["post_stage_ms"], 1e-9))
+    del d_in, d_flags
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_density(args):
+    """Live rows and the nonzero density of the live rows' activations after
+    each of the first layers (the inputs of the next layer), stepping one
+    engine's layers with the one-layer entry point on seeded rows -- the
+    figures that decide whether skipping zero inputs could beat the gather."""
+    import ctypes
+    import torch
+    import snicit_gb300 as sg
+    N, L, B, bias, _ = WORKLOADS[args.workload]
+    rows = min(args.density_rows, 65536)
+    K = min(args.density_layers, L)
+    lib = sg.load()
+    x = torch.empty((rows, N), dtype=torch.float32, device="cuda")
+    sg.generate_inputs_device(N, SEED, 0, rows, x.data_ptr())
+    y = torch.empty_like(x)
+    alive = torch.empty(rows, dtype=torch.int32, device="cuda")
+    out = {"workload": args.workload, "rows": rows, "layers": []}
+    with sg.Engine(N, K, mode="SNIG", batch=rows, bias=bias) as eng:
+        eng.generate_weights(SEED, NNZ, 0.0625)
+        eng.finalize()
+        live_in = rows
+        out["input_density"] = float((x > 0).float().mean())
+        for l in range(K):
+            rc = lib.sdnn_layer_noalloc(eng._h, l, ctypes.c_void_p(x.data_ptr()),
+                                        ctypes.c_void_p(y.data_ptr()), rows,
+                                        ctypes.c_void_p(alive.data_ptr()), None)
+            assert rc == 0, lib.sdnn_last_error(eng._h)
+            torch.cuda.synchronize()
+            m = alive > 0
+            live = int(m.sum())
+            yl = y[m]
+            dens = float((yl > 0).float().mean()) if live else 0.0
+            sat = float((yl >= 32.0).float().mean()) if live else 0.0
+            out["layers"].append({"layer": l, "rows_in": live_in, "rows_out": live,
+                                  "out_density": dens, "saturated": sat})
+            live_in = live
+            x, y = y, x
+    print(json.dumps({"density": out}), flush=True)
 
 
 def run_extra(args, sg, torch, workload, local):
@@ -758,6 +852,14 @@ def main():
     ap.add_argument("--no-uneven", action="store_true",
                     help="skip the twelve uneven batches (one schedule vs one by one)")
     ap.add_argument("--no-extra", action="store_true", help="skip the extra workloads")
+    ap.add_argument("--no-residue", action="store_true",
+                    help="skip the residue-stage measurement (4096 x 480 clustered at layer 6)")
+    ap.add_argument("--residue-only", action="store_true",
+                    help="only the residue-stage measurement")
+    ap.add_argument("--density", action="store_true",
+                    help="live rows and activation density per layer of --workload")
+    ap.add_argument("--density-rows", type=int, default=8192)
+    ap.add_argument("--density-layers", type=int, default=12)
     ap.add_argument("--extra-workloads", default="sdgc-4096x480",
                     help="comma-separated workloads reported as extra keys")
     ap.add_argument("--e2e-steps", type=int, default=5,
@@ -772,6 +874,12 @@ def main():
     args = ap.parse_args()
     if args.case:
         run_case(args)
+    elif args.density:
+        run_density(args)
+    elif args.residue_only:
+        import torch
+        import snicit_gb300 as sg
+        print(json.dumps({"residue_stage": run_residue(args, sg, torch, 0)}), flush=True)
     elif args.serve_only:
         import snicit_gb300 as sg
         print(json.dumps({"serving": run_serving(args, sg)}), flush=True)

@@ -247,8 +247,9 @@ int sdnn_infer_batches_device(sdnn_engine* e, const float* const* d_inputs, cons
 int sdnn_read_inputs_tsv(const char* path, int32_t num_neurons, int64_t row_offset,
                          int64_t rows, float* out);
 
-/* Final activations of the last inference, rows x N, neuron order of the
- * reference (SNICIT rows are recovered: centroid + residue). */
+/* Final activations of the first `rows` rows of the last inference (at most
+ * its row count), rows x N, neuron order of the reference (SNICIT rows are
+ * recovered: centroid + residue). */
 int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows);
 
 /* Statistics of the last inference. */

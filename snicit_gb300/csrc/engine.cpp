@@ -2091,7 +2091,8 @@ int sdnn_infer_batches_device(sdnn_engine* e, const float* const* d_inputs, cons
 int sdnn_read_activations(sdnn_engine* e, float* out, int64_t rows) {
   if (!e || !out) return SDNN_ERR_INVALID;
   if (!e->have_run) return fail(e, SDNN_ERR_STATE, "no inference has run");
-  if (rows != e->last_rows) return fail(e, SDNN_ERR_INVALID, "rows differ from the last batch");
+  if (rows <= 0 || rows > e->last_rows)
+    return fail(e, SDNN_ERR_INVALID, "rows exceed the last batch");
   cudaSetDevice(e->dev);
   const int L = e->L;
   float* scratch = e->d_y[L & 1];
