@@ -820,7 +820,11 @@ def run_case(args):
     eng = sg.Engine(N, L, mode=mode, threshold=t, batch=B, bias=sg.load().sdnn_reference_bias(N),
                     num_centroids=args.centroids, tile_rows=args.tile, threads=args.threads,
                     merge_start=args.merge_start, merge_every=args.merge_every,
-                    merge=not args.case.startswith("residue"))
+                    merge=not args.case.startswith("residue"),
+                    # ncu cannot profile kernels inside a graph with a conditional
+                    # node: the residue cases let the host choose the post path
+                    device_post_choice=not args.case.startswith("residue"),
+                    sparse_residue=not args.dense_residue)
     eng.generate_weights(SEED, NNZ, 0.0625)
     for _ in range(2):
         eng.infer(Y0)
@@ -856,6 +860,8 @@ def main():
                     help="skip the residue-stage measurement (4096 x 480 clustered at layer 6)")
     ap.add_argument("--residue-only", action="store_true",
                     help="only the residue-stage measurement")
+    ap.add_argument("--dense-residue", action="store_true",
+                    help="cases: every residue row stays dense (no sparse lists)")
     ap.add_argument("--density", action="store_true",
                     help="live rows and activation density per layer of --workload")
     ap.add_argument("--density-rows", type=int, default=8192)

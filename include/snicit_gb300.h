@@ -140,7 +140,7 @@ typedef struct sdnn_stats {
   int32_t device_post_choice; /* SNICIT: 1 when the post-threshold path was chosen on
                             the device (the whole inference one graph launch)     */
   int32_t sparse_residue_rows; /* SNICIT: residue rows at the threshold kept as sparse
-                            (position, value) lists (<= N/8 nonzeros)             */
+                            (position, value) lists (<= max(32, N/32) nonzeros)  */
   int64_t sparse_row_layers;   /* sparse residue rows summed over the post layers   */
 } sdnn_stats;
 

@@ -194,7 +194,7 @@ struct sdnn_engine {
   // d_slist[p & 1] with their entries in d_sp*[p & 1]; d_rtmp collects the
   // non-empty rows of a dense residue launch before they are split
   bool sparse_res = false;
-  int32_t sp_cap = 0;  // entries per sparse row (N / 8)
+  int32_t sp_cap = 0;  // entries per sparse row (N / 32, at least 32)
   int32_t* d_sp_idx[2] = {nullptr, nullptr};
   float* d_sp_val[2] = {nullptr, nullptr};
   int32_t* d_sp_cnt[2] = {nullptr, nullptr};
@@ -469,7 +469,9 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
   if (e->sparse_res) {
-    e->sp_cap = std::max(1, e->N / 8);
+    // a sparse row's update runs on one warp, entry after entry: rows with
+    // more than N / 32 nonzeros stay dense (the gather kernel's throughput)
+    e->sp_cap = std::max(32, e->N / 32);
     for (int i = 0; i < 2; ++i) {
       T(A(&e->d_sp_idx[i], (size_t)cap * e->sp_cap * 4));
       T(A(&e->d_sp_val[i], (size_t)cap * e->sp_cap * 4));
@@ -747,9 +749,41 @@ int for_layers(sdnn_engine* e, Fn fn) {
   return status.load();
 }
 
-// Neuron placement of every layer into e->pos (whole-row layouts): outputs
-// grouped by in-degree, lanes balancing the next layer's bank loads.
+// Neuron placement of every layer into e->pos.  Whole rows: outputs grouped
+// by in-degree, lanes balancing the next layer's bank loads.  Input chunks:
+// each neuron's chunk balancing the next layer's per-chunk in-degrees, groups
+// of outputs with similar per-chunk in-degrees, lanes balancing the next
+// layer's (group, chunk, bank) loads.
+int compute_placement_chunked(sdnn_engine* e) {
+  const int L = e->L;
+  std::vector<std::vector<uint8_t>> chunk(L);
+  int rc = for_layers(e, [&](int l, std::string&) {
+    HostLayer tmp;
+    const HostLayer* next = l + 1 < L ? host_layer(e, l + 1, tmp) : nullptr;
+    chunk[l] = chunk_assign(next, e->N, e->Q, 0x5EED0000ull + (uint64_t)l);
+    return SDNN_OK;
+  });
+  if (rc) return rc;
+  std::vector<std::vector<int32_t>> order(L);
+  rc = for_layers(e, [&](int l, std::string&) {
+    HostLayer tmp;
+    order[l] = chunk_group_order(*host_layer(e, l, tmp), l > 0 ? chunk[l - 1].data() : nullptr,
+                                 chunk[l], e->N, e->Q);
+    return SDNN_OK;
+  });
+  if (rc) return rc;
+  e->pos.assign(L, {});
+  return for_layers(e, [&](int l, std::string&) {
+    HostLayer tmp;
+    const HostLayer* next = l + 1 < L ? host_layer(e, l + 1, tmp) : nullptr;
+    e->pos[l] = place_outputs_chunked(order[l], chunk[l], next, next ? &order[l + 1] : nullptr,
+                                      e->N, e->Q);
+    return SDNN_OK;
+  });
+}
+
 int compute_placement(sdnn_engine* e) {
+  if (e->nq > 1) return compute_placement_chunked(e);
   std::vector<std::vector<int32_t>> order(e->L);
   int rc = for_layers(e, [&](int l, std::string&) {
     HostLayer tmp;
@@ -782,7 +816,7 @@ int finalize_weights(sdnn_engine* e) {
   free_weights(e);
   e->dl.assign(e->L, DevLayer{});
   e->pos.clear();
-  const bool place = !e->packed && e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
+  const bool place = !e->packed && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
   int rc;
   if (e->packed) {
     // a packed-weight file: its placement and slots as they are, checked first
@@ -2136,7 +2170,7 @@ int sdnn_save_packed_weights(sdnn_engine* e, const char* path) {
       if (!e->hw[l].present)
         return fail(e, SDNN_ERR_STATE, "layer " + std::to_string(l) + " has no weights");
   }
-  const bool place = e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
+  const bool place = !(e->cfg.flags & SDNN_FLAG_NO_PLACEMENT);
   int rc;
   if (place) {
     if ((rc = compute_placement(e))) return rc;

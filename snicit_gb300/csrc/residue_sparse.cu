@@ -5,8 +5,9 @@
 // centroid, Delta keeps only a few nonzeros; the reference's post_spMM then
 // skips the zero entries of the residue (kernel.hpp:71-102, `if (val != 0)`),
 // but its post_minus still walks every output (kernel.hpp:104-136).  Here a
-// residue row with at most SC = N/8 nonzeros is kept as a sorted (position,
-// value) list and its update touches only what it must:
+// residue row with at most SC nonzeros (N/32, at least 32: a sparse row's
+// update runs on one warp, so longer lists would stretch the layer) is kept as
+// a sorted (position, value) list and its update touches only what it must:
 //
 //   split_residue_kernel   residue conversion: one warp per dense residue row,
 //                          warp ballot / popc compaction of the nonzeros into
@@ -76,37 +77,60 @@ __global__ void sparse_residue_kernel(const SparseResArgs a) {
   extern __shared__ __align__(16) float sm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
   const int N = a.N, nwords = N >> 5, SC = a.in.cap;
+  const int n = *a.count_in;
+  if ((int)blockIdx.x * wpc >= n) return;  // no row for this CTA (often no row at all)
   float* acc = sm + (size_t)warp * (N + nwords);
   uint32_t* bm = reinterpret_cast<uint32_t*>(acc + N);
   for (int j = lane; j < N + nwords; j += 32) acc[j] = 0.f;  // also clears the bitmap
   __syncwarp();
   const float hi = a.clampv;
-  const int n = *a.count_in;
   for (int i = blockIdx.x * wpc + warp; i < n; i += gridDim.x * wpc) {
     const int r = a.list_in[i];
     const int cnt = a.in.cnt[r];
     const int32_t* ei = a.in.idx + (size_t)r * SC;
     const float* ev = a.in.val + (size_t)r * SC;
-    // W * Delta: entries in ascending position, each along its out-edges
+    // W * Delta: entries in ascending position, each along its out-edges.
+    // Lane e holds entry e0 + e and its edge range; the edges of four entries
+    // are loaded before the first of them is applied (the loads do not depend
+    // on one another), the multiply-adds stay in entry order.
     for (int e0 = 0; e0 < cnt; e0 += 32) {
-      int my_j = 0;
+      int my_j = 0, my_t0 = 0, my_t1 = 0;
       float my_v = 0.f;
       if (e0 + lane < cnt) {
         my_j = ei[e0 + lane];
         my_v = ev[e0 + lane];
+        my_t0 = __ldg(a.tr_off + my_j);
+        my_t1 = __ldg(a.tr_off + my_j + 1);
       }
       const int ne = min(32, cnt - e0);
-      for (int e = 0; e < ne; ++e) {
-        const int j = __shfl_sync(kFull, my_j, e);
-        const float v = __shfl_sync(kFull, my_v, e);
-        const int t1 = __ldg(a.tr_off + j + 1);
-        for (int t = __ldg(a.tr_off + j) + lane; t < t1; t += 32) {
-          const int o = __ldg(a.tr_out + t);
-          const float w = a.tr_val ? __ldg(a.tr_val + t) : a.wconst;
-          acc[o] = fmaf(w, v, acc[o]);
-          atomicOr(&bm[o >> 5], 1u << (o & 31));
+      for (int e = 0; e < ne; e += 4) {
+        int o[4];
+        float w[4], v[4];
+        int deg[4], t0[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int src = min(e + u, ne - 1);
+          t0[u] = __shfl_sync(kFull, my_t0, src);
+          deg[u] = e + u < ne ? __shfl_sync(kFull, my_t1, src) - t0[u] : 0;
+          v[u] = __shfl_sync(kFull, my_v, src);
+          o[u] = lane < deg[u] ? (int)__ldg(a.tr_out + t0[u] + lane) : -1;
+          w[u] = a.tr_val && lane < deg[u] ? __ldg(a.tr_val + t0[u] + lane) : a.wconst;
         }
-        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (o[u] >= 0) {
+            acc[o[u]] = fmaf(w[u], v[u], acc[o[u]]);
+            atomicOr(&bm[o[u] >> 5], 1u << (o[u] & 31));
+          }
+          // out-degrees above 32 (general layers): the rest of the edges
+          for (int t = t0[u] + 32 + lane; t < t0[u] + deg[u]; t += 32) {
+            const int oo = __ldg(a.tr_out + t);
+            const float ww = a.tr_val ? __ldg(a.tr_val + t) : a.wconst;
+            acc[oo] = fmaf(ww, v[u], acc[oo]);
+            atomicOr(&bm[oo >> 5], 1u << (oo & 31));
+          }
+          __syncwarp();
+        }
       }
     }
     const float* pre = a.pre + (size_t)a.cslot[r] * N;

@@ -330,4 +330,139 @@ bool pack_layer(const HostLayer& h, int32_t N, int32_t Q, int32_t scale, PackedL
   return true;
 }
 
+
+// ---- neuron placement for input-chunked layouts ---------------------------
+//
+// With input chunks a slot list belongs to one (group, chunk): it is as deep
+// as the busiest lane (an output's in-edges from that chunk) or bank (the
+// group's in-edges from that chunk landing in one bank).  Three steps spread
+// both, each a pure function of the layers (so they run for all layers at
+// once): which chunk a neuron sits in, which outputs share a group, and each
+// neuron's lane inside its group.
+
+namespace {
+uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+}  // namespace
+
+std::vector<uint8_t> chunk_assign(const HostLayer* next, int32_t N, int32_t Q, uint64_t seed) {
+  const int32_t nq = N / Q;
+  std::vector<uint8_t> chunk(N);
+  if (!next) {
+    for (int32_t n = 0; n < N; ++n) chunk[n] = (uint8_t)(n / Q);
+    return chunk;
+  }
+  // neurons in a seeded order (Fisher-Yates on a SplitMix64 stream); each goes
+  // to the chunk with room that adds the least squared count to the (output of
+  // the next layer, chunk) pairs it feeds
+  std::vector<int32_t> order(N);
+  std::iota(order.begin(), order.end(), 0);
+  for (int32_t i = N - 1; i > 0; --i) {
+    const uint64_t r = mix64(seed + (uint64_t)i * 0x9E3779B97F4A7C15ull);
+    std::swap(order[i], order[(int32_t)(r % (uint64_t)(i + 1))]);
+  }
+  std::vector<int32_t> cnt((size_t)N * nq, 0), room(nq, Q);
+  for (int32_t n : order) {
+    int best = -1;
+    int64_t best_cost = INT64_MAX;
+    for (int q = 0; q < nq; ++q) {
+      if (!room[q]) continue;
+      int64_t cost = 0;
+      for (int32_t k = next->row_off[n]; k < next->row_off[n + 1]; ++k)
+        cost += 2 * cnt[(size_t)next->cols[k] * nq + q] + 1;
+      if (cost < best_cost) {
+        best_cost = cost;
+        best = q;
+      }
+    }
+    chunk[n] = (uint8_t)best;
+    room[best]--;
+    for (int32_t k = next->row_off[n]; k < next->row_off[n + 1]; ++k)
+      cnt[(size_t)next->cols[k] * nq + best]++;
+  }
+  return chunk;
+}
+
+std::vector<int32_t> chunk_group_order(const HostLayer& h, const uint8_t* in_chunk,
+                                       const std::vector<uint8_t>& out_chunk, int32_t N,
+                                       int32_t Q) {
+  const int32_t nq = N / Q;
+  // in-degree of every output per input chunk
+  std::vector<int32_t> deg((size_t)N * nq, 0);
+  for (int32_t j = 0; j < N; ++j) {
+    const int q = in_chunk ? in_chunk[j] : j / Q;
+    for (int32_t k = h.row_off[j]; k < h.row_off[j + 1]; ++k) deg[(size_t)h.cols[k] * nq + q]++;
+  }
+  auto key = [&](int32_t n) {
+    int32_t mx = 0, sum = 0;
+    for (int q = 0; q < nq; ++q) {
+      mx = std::max(mx, deg[(size_t)n * nq + q]);
+      sum += deg[(size_t)n * nq + q];
+    }
+    return std::make_pair(mx, sum);
+  };
+  std::vector<int32_t> order;
+  order.reserve(N);
+  for (int q = 0; q < nq; ++q) {
+    std::vector<int32_t> in_q;
+    for (int32_t n = 0; n < N; ++n)
+      if (out_chunk[n] == q) in_q.push_back(n);
+    // outputs of similar per-chunk depth share a group: largest chunk degree,
+    // then total in-degree, descending
+    std::stable_sort(in_q.begin(), in_q.end(), [&](int32_t a, int32_t b) { return key(a) > key(b); });
+    order.insert(order.end(), in_q.begin(), in_q.end());
+  }
+  return order;
+}
+
+std::vector<int32_t> place_outputs_chunked(const std::vector<int32_t>& order,
+                                           const std::vector<uint8_t>& out_chunk,
+                                           const HostLayer* next,
+                                           const std::vector<int32_t>* next_order, int32_t N,
+                                           int32_t Q) {
+  std::vector<int32_t> pos(N);
+  const int32_t G = N / 32, nq = N / Q;
+  if (!next || !next_order) {
+    for (int32_t i = 0; i < N; ++i) pos[order[i]] = i;
+    return pos;
+  }
+  std::vector<int32_t> gnext(N);
+  for (int32_t i = 0; i < N; ++i) gnext[(*next_order)[i]] = i / 32;
+  // bank loads of the next layer per (group, chunk, bank); the cost of a load
+  // grows as 4^load so the greedy keeps the largest load of a list down
+  std::vector<int32_t> load((size_t)G * nq * 32, 0);
+  auto weight = [](int32_t x) -> int64_t { return (int64_t)1 << (2 * std::min(x, 28)); };
+  std::vector<int32_t> nodes(32);
+  for (int32_t g = 0; g < G; ++g) {
+    for (int i = 0; i < 32; ++i) nodes[i] = order[32 * g + i];
+    std::stable_sort(nodes.begin(), nodes.end(), [&](int32_t a, int32_t b) {
+      return next->row_off[a + 1] - next->row_off[a] > next->row_off[b + 1] - next->row_off[b];
+    });
+    uint32_t used = 0;
+    for (int32_t n : nodes) {
+      const size_t q = out_chunk[n];
+      int best = -1;
+      int64_t best_cost = INT64_MAX;
+      for (int b = 0; b < 32; ++b) {
+        if (used & (1u << b)) continue;
+        int64_t cost = 0;
+        for (int32_t k = next->row_off[n]; k < next->row_off[n + 1]; ++k)
+          cost += weight(load[((size_t)gnext[next->cols[k]] * nq + q) * 32 + b]);
+        if (cost < best_cost) {
+          best_cost = cost;
+          best = b;
+        }
+      }
+      used |= 1u << best;
+      pos[n] = 32 * g + best;
+      for (int32_t k = next->row_off[n]; k < next->row_off[n + 1]; ++k)
+        load[((size_t)gnext[next->cols[k]] * nq + q) * 32 + best]++;
+    }
+  }
+  return pos;
+}
+
 }  // namespace sdnn

@@ -59,4 +59,24 @@ std::vector<int32_t> degree_order(const HostLayer& h, int32_t N);
 std::vector<int32_t> place_outputs(const std::vector<int32_t>& order, const HostLayer* next,
                                    const std::vector<int32_t>* next_order, int32_t N);
 
+
+// Placement for input-chunked layouts (chunks of Q inputs):
+//  chunk_assign: the chunk of every output neuron of a layer (Q per chunk),
+//    balancing the in-edges of every output of the next layer over the chunks
+//    (next == nullptr: neuron n in chunk n / Q); seeded, deterministic;
+//  chunk_group_order: the layer's output groups -- chunk by chunk, outputs of
+//    similar per-input-chunk in-degree together (in_chunk: chunk of each input,
+//    nullptr = j / Q); group g is order[32g .. 32g+31], inside chunk 32g / Q;
+//  place_outputs_chunked: each output's lane in its group, balancing the next
+//    layer's (group, chunk, bank) loads.
+std::vector<uint8_t> chunk_assign(const HostLayer* next, int32_t N, int32_t Q, uint64_t seed);
+std::vector<int32_t> chunk_group_order(const HostLayer& h, const uint8_t* in_chunk,
+                                       const std::vector<uint8_t>& out_chunk, int32_t N,
+                                       int32_t Q);
+std::vector<int32_t> place_outputs_chunked(const std::vector<int32_t>& order,
+                                           const std::vector<uint8_t>& out_chunk,
+                                           const HostLayer* next,
+                                           const std::vector<int32_t>* next_order, int32_t N,
+                                           int32_t Q);
+
 }  // namespace sdnn

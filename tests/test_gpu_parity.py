@@ -646,7 +646,7 @@ def test_plain_path_is_bitwise_equal_to_slot_order_evaluation(tmp_path, N, L, B,
     assert np.array_equal(Y[alive].view(np.uint32), want[alive].view(np.uint32))
 
 
-@pytest.mark.parametrize("N,L,B,T,K", [(1024, 40, 600, 6, 16), (4096, 30, 200, 7, 32),
+@pytest.mark.parametrize("N,L,B,T,K", [(1024, 40, 600, 6, 16), (4096, 60, 400, 8, 32),
                                        (256, 40, 500, 4, 8)])
 def test_sparse_residue_rows_match_dense_rows_and_oracle(N, L, B, T, K):
     """Residue rows that keep few nonzeros become sparse (position, value)

@@ -121,9 +121,12 @@ def test_slots_share_the_model_weights_and_grow_at_admission():
     layers, hw, hb = sg.sparse_mlp(seed, L=12)
     big = sg.mlp_inputs(seed, 0, 10000)
     small = sg.mlp_inputs(seed, 1, 37)
+    with sg.Engine(N, len(layers), mode="SNIG", batch=len(big), bias=-0.05) as ref:
+        for l, (ro, c, v) in enumerate(layers):
+            ref.set_layer_csr(l, ro, c, v)
+        f_big, _ = ref.infer(big)
+        y_big = ref.activations(len(big))
     with _engine(layers, N) as eng:
-        f_big, _ = eng.infer(big)
-        y_big = eng.activations(len(big))
         with sg.Server(eng, hw, hb, slots=3, max_rows=16384) as sv:
             st0 = sv.stats()
             assert st0["slot_rows"] == 4096
