@@ -19,6 +19,7 @@ namespace sdnn {
 int engine_set_tile(sdnn_engine* e, int tile_rows, int threads);
 void engine_set_snicit(sdnn_engine* e, int threshold, int centroids);
 void engine_set_merge(sdnn_engine* e, int start, int every, bool on);
+bool engine_set_sparse(sdnn_engine* e, bool on);
 sdnn_config engine_config(const sdnn_engine* e);
 }  // namespace sdnn
 
@@ -138,6 +139,18 @@ int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
     }
     if (bs.ms < 1e30f) sdnn::engine_set_snicit(e, bs.threshold, bs.centroids);
     else sdnn::engine_set_snicit(e, cfg0.threshold, cfg0.num_centroids);
+    // residue rows at the chosen threshold: sparse residue lists or dense rows
+    // only, whichever is faster on the sample
+    if (bs.ms < 1e30f && bs.threshold < cfg0.num_layers) {
+      const bool sparse0 = !(cfg0.flags & SDNN_FLAG_DENSE_RESIDUE);
+      if (sdnn::engine_set_sparse(e, !sparse0) != sparse0) {
+        Trial t = bs;
+        t.status = time_setting(e, smp, -1, t.ms, t.survivors);
+        record(f, sparse0 ? "dense_residue" : "sparse_residue", t, smp.rows);
+        if (t.status == SDNN_OK && t.ms < bs.ms) bs = t;
+        else sdnn::engine_set_sparse(e, sparse0);
+      }
+    }
     if (merge_on && bs.ms < 1e30f) {
       // first layer after which identical rows are merged: early merging finds
       // duplicates sooner, late merging skips hashing rows that are all distinct;

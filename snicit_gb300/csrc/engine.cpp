@@ -193,7 +193,8 @@ struct sdnn_engine {
   // p the dense residue rows are d_rlist[p & 1] and the sparse ones
   // d_slist[p & 1] with their entries in d_sp*[p & 1]; d_rtmp collects the
   // non-empty rows of a dense residue launch before they are split
-  bool sparse_res = false;
+  bool sparse_built = false;  // transposed layers and sparse lists allocated
+  bool sparse_res = false;    // ... and used
   int32_t sp_cap = 0;  // entries per sparse row (N / 32, at least 32)
   int32_t* d_sp_idx[2] = {nullptr, nullptr};
   float* d_sp_val[2] = {nullptr, nullptr};
@@ -371,8 +372,10 @@ void choose_layout(sdnn_engine* e) {
   e->nq = N / e->Q;
   e->G = N / 32;
   // sparse residue rows need the whole row of one warp in shared memory
-  e->sparse_res = e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_DENSE_RESIDUE) &&
-                  sparse_residue_warps(N) > 0;
+  // (the transposed layers and the lists exist whenever the layout allows
+  // them, so the autotuner may switch between sparse and dense rows)
+  e->sparse_built = e->nq == 1 && sparse_residue_warps(N) > 0;
+  e->sparse_res = e->sparse_built && !(e->cfg.flags & SDNN_FLAG_DENSE_RESIDUE);
 }
 
 int choose_kernel(sdnn_engine* e) {
@@ -468,7 +471,7 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
   T(A(&e->d_ids, (size_t)cap * 4));
   T(A(&e->d_idcount, 16));
   T(A(&e->d_fallback, (size_t)cap * 4));
-  if (e->sparse_res) {
+  if (e->sparse_built) {
     // a sparse row's update runs on one warp, entry after entry: rows with
     // more than N / 32 nonzeros stay dense (the gather kernel's throughput)
     e->sp_cap = std::max(32, e->N / 32);
@@ -655,7 +658,7 @@ int upload_layer(sdnn_engine* e, int l, const PackedView& p, std::string& err) {
     T(cudaMalloc((void**)&d.sums, sizeof(sums)));
     if (rc == cudaSuccess) T(cudaMemcpy(d.sums, sums, sizeof(sums), cudaMemcpyHostToDevice));
   }
-  if (rc == cudaSuccess && e->sparse_res && e->nq == 1) {
+  if (rc == cudaSuccess && e->sparse_built) {
     // out-edges of every input position, from the packed slots (padding slots
     // point past the chunk and are skipped), each input's edges by output
     const int32_t scale = slot_index_in_bytes(e->Q) ? 4 : 1;
@@ -1543,7 +1546,7 @@ int prepare(sdnn_engine* e, int64_t rows) {
   }
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, true}, e->smem));
   CK(layer_prepare(LayerKernelKey{e->key.T, e->key.rsw, e->key.kg, false}, e->smem));
-  if (e->sparse_res) CK(sparse_residue_prepare(e->N));
+  if (e->sparse_built) CK(sparse_residue_prepare(e->N));
   e->bits_chunked = e->nq > 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
                     layer0_bits_chunked_supported(e->N, e->Q);
   e->bits_grid = (e->nq == 1 && !(e->cfg.flags & SDNN_FLAG_NO_BINARY_FIRST_LAYER) &&
@@ -2304,6 +2307,18 @@ void engine_set_snicit(sdnn_engine* e, int threshold, int centroids) {
     if (centroids > e->Kcap) free_buffers(e);  // the centroid buffers hold Kcap rows
   }
   drop_graph(e);
+}
+// Sparse residue lists on or off (the layout must allow them); returns
+// whether they are on.
+bool engine_set_sparse(sdnn_engine* e, bool on) {
+  const bool want = on && e->sparse_built;
+  e->cfg.flags = on ? (e->cfg.flags & ~SDNN_FLAG_DENSE_RESIDUE)
+                    : (e->cfg.flags | SDNN_FLAG_DENSE_RESIDUE);
+  if (want != e->sparse_res) {
+    e->sparse_res = want;
+    drop_graph(e);
+  }
+  return e->sparse_res;
 }
 void engine_set_merge(sdnn_engine* e, int start, int every, bool on) {
   e->cfg.merge_start = start;

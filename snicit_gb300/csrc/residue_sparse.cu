@@ -34,13 +34,39 @@ namespace sdnn {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kAhead = 8;  // entries whose edges are in flight at once
 
 __device__ __forceinline__ float clamp_hi(float v, float hi) { return fminf(hi, fmaxf(0.f, v)); }
+
+// Launched with programmatic stream serialization (like the layer kernel):
+// the next launch may be scheduled now; everything this kernel reads comes
+// from its predecessors, so it waits for them before the first read.
+__device__ __forceinline__ void pdl_prologue() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... Args>
+cudaError_t launch_pdl(void (*fn)(Args...), int grid, int threads, size_t smem, cudaStream_t s,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, args...);
+}
 
 __global__ void split_residue_kernel(const float* __restrict__ y, const int32_t* list,
                                      const int32_t* count, SparseRows out, int32_t* dense_list,
                                      int32_t* dense_count, int32_t* sparse_list,
                                      int32_t* sparse_count, int32_t N) {
+  pdl_prologue();
   const int n = *count;
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -48,19 +74,45 @@ __global__ void split_residue_kernel(const float* __restrict__ y, const int32_t*
   const int SC = out.cap;
   for (int i = wid; i < n; i += nw) {
     const int r = list[i];
-    const float* yr = y + (size_t)r * N;
+    const float4* yr = reinterpret_cast<const float4*>(y + (size_t)r * N);
     int32_t* oi = out.idx + (size_t)r * SC;
     float* ov = out.val + (size_t)r * SC;
     int base = 0;
-    for (int j0 = 0; j0 < N && base <= SC; j0 += 32) {
-      const float v = yr[j0 + lane];
-      const unsigned m = __ballot_sync(kFull, v != 0.f);
-      const int k = base + __popc(m & ((1u << lane) - 1u));
-      if (v != 0.f && k < SC) {
-        oi[k] = j0 + lane;
-        ov[k] = v;
+    // 256 entries per round: lane L holds entries j0 + 4L .. j0 + 4L + 3 of
+    // each 128-entry half (both halves loaded before either is compacted);
+    // a lane's nonzeros go after those of the lanes below it, so the list
+    // comes out in ascending position
+    for (int j0 = 0; j0 < N && base <= SC; j0 += 256) {
+      float4 v[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int j = j0 + 128 * h + 4 * lane;
+        v[h] = j < N ? yr[j >> 2] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      base += __popc(m);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float e[4] = {v[h].x, v[h].y, v[h].z, v[h].w};
+        const int nz = (e[0] != 0.f) + (e[1] != 0.f) + (e[2] != 0.f) + (e[3] != 0.f);
+        int incl = nz;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int u = __shfl_up_sync(kFull, incl, d);
+          if (lane >= d) incl += u;
+        }
+        int k = base + incl - nz;
+        const int j = j0 + 128 * h + 4 * lane;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (e[t] != 0.f) {
+            if (k < SC) {
+              oi[k] = j + t;
+              ov[k] = e[t];
+            }
+            ++k;
+          }
+        }
+        base += __shfl_sync(kFull, incl, 31);
+      }
     }
     if (lane == 0) {
       if (base <= SC) {
@@ -77,6 +129,7 @@ __global__ void sparse_residue_kernel(const SparseResArgs a) {
   extern __shared__ __align__(16) float sm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
   const int N = a.N, nwords = N >> 5, SC = a.in.cap;
+  pdl_prologue();
   const int n = *a.count_in;
   if ((int)blockIdx.x * wpc >= n) return;  // no row for this CTA (often no row at all)
   float* acc = sm + (size_t)warp * (N + nwords);
@@ -90,9 +143,9 @@ __global__ void sparse_residue_kernel(const SparseResArgs a) {
     const int32_t* ei = a.in.idx + (size_t)r * SC;
     const float* ev = a.in.val + (size_t)r * SC;
     // W * Delta: entries in ascending position, each along its out-edges.
-    // Lane e holds entry e0 + e and its edge range; the edges of four entries
-    // are loaded before the first of them is applied (the loads do not depend
-    // on one another), the multiply-adds stay in entry order.
+    // Lane e holds entry e0 + e and its edge range; the edges of kAhead
+    // entries are loaded before the first of them is applied (the loads do not
+    // depend on one another), the multiply-adds stay in entry order.
     for (int e0 = 0; e0 < cnt; e0 += 32) {
       int my_j = 0, my_t0 = 0, my_t1 = 0;
       float my_v = 0.f;
@@ -103,12 +156,12 @@ __global__ void sparse_residue_kernel(const SparseResArgs a) {
         my_t1 = __ldg(a.tr_off + my_j + 1);
       }
       const int ne = min(32, cnt - e0);
-      for (int e = 0; e < ne; e += 4) {
-        int o[4];
-        float w[4], v[4];
-        int deg[4], t0[4];
+      for (int e = 0; e < ne; e += kAhead) {
+        int o[kAhead];
+        float w[kAhead], v[kAhead];
+        int deg[kAhead], t0[kAhead];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kAhead; ++u) {
           const int src = min(e + u, ne - 1);
           t0[u] = __shfl_sync(kFull, my_t0, src);
           deg[u] = e + u < ne ? __shfl_sync(kFull, my_t1, src) - t0[u] : 0;
@@ -117,7 +170,7 @@ __global__ void sparse_residue_kernel(const SparseResArgs a) {
           w[u] = a.tr_val && lane < deg[u] ? __ldg(a.tr_val + t0[u] + lane) : a.wconst;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kAhead; ++u) {
           if (o[u] >= 0) {
             acc[o[u]] = fmaf(w[u], v[u], acc[o[u]]);
             atomicOr(&bm[o[u] >> 5], 1u << (o[u] & 31));
@@ -210,6 +263,7 @@ __global__ void sparse_residue_kernel(const SparseResArgs a) {
 
 __global__ void densify_kernel(const int32_t* list, const int32_t* count, SparseRows rows,
                                float* y, int32_t N) {
+  pdl_prologue();
   const int n = *count;
   const int lane = threadIdx.x & 31;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -249,8 +303,8 @@ void launch_split_residue(const float* y, const int32_t* list, const int32_t* co
                           const SparseRows& out, int32_t* dense_list, int32_t* dense_count,
                           int32_t* sparse_list, int32_t* sparse_count, int32_t N, int num_sms,
                           cudaStream_t s) {
-  split_residue_kernel<<<num_sms * 8, 256, 0, s>>>(y, list, count, out, dense_list, dense_count,
-                                                    sparse_list, sparse_count, N);
+  launch_pdl(split_residue_kernel, num_sms * 8, 256, 0, s, y, list, count, out, dense_list,
+             dense_count, sparse_list, sparse_count, N);
 }
 
 cudaError_t launch_sparse_residue(const SparseResArgs& a, int num_sms, cudaStream_t s) {
@@ -259,13 +313,12 @@ cudaError_t launch_sparse_residue(const SparseResArgs& a, int num_sms, cudaStrea
   const size_t smem = w * sparse_residue_smem_per_warp(a.N);
   int per_sm = (int)((227 * 1024) / (smem + 1024));
   per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
-  sparse_residue_kernel<<<num_sms * per_sm, w * 32, smem, s>>>(a);
-  return cudaGetLastError();
+  return launch_pdl(sparse_residue_kernel, num_sms * per_sm, w * 32, smem, s, a);
 }
 
 void launch_densify(const int32_t* list, const int32_t* count, const SparseRows& rows, float* y,
                     int32_t N, int num_sms, cudaStream_t s) {
-  densify_kernel<<<num_sms * 4, 256, 0, s>>>(list, count, rows, y, N);
+  launch_pdl(densify_kernel, num_sms * 4, 256, 0, s, list, count, rows, y, N);
 }
 
 }  // namespace sdnn
