@@ -324,7 +324,8 @@ def run_ours(args):
     eng = sg.Engine(N, L, mode="SNICIT", threshold=threshold, batch=rows_all, bias=bias,
                     num_centroids=args.centroids, device=local, tile_rows=args.tile,
                     threads=args.threads, merge_start=args.merge_start,
-                    merge_every=args.merge_every)
+                    merge_every=args.merge_every,
+                    device_post_choice=not args.host_post_choice)
     t0 = time.perf_counter()
     weights = load_weights(eng, args, N, L)
     pack_s = time.perf_counter() - t0
@@ -860,6 +861,9 @@ def main():
                     help="skip the residue-stage measurement (4096 x 480 clustered at layer 6)")
     ap.add_argument("--residue-only", action="store_true",
                     help="only the residue-stage measurement")
+    ap.add_argument("--host-post-choice", action="store_true",
+                    help="the host picks the post-threshold path (phase graphs without a "
+                         "conditional node, whose kernels ncu can profile)")
     ap.add_argument("--dense-residue", action="store_true",
                     help="cases: every residue row stays dense (no sparse lists)")
     ap.add_argument("--density", action="store_true",

@@ -117,9 +117,7 @@ __global__ void __launch_bounds__(kGridChainThreads) chain_grid_kernel(const Gri
       const int nb = __shfl_sync(0xffffffffu, bnd, nq) - g0;
       const uint2* ip = wl.idx + (size_t)g0 * 32 + lane;
       const float4* vp = wl.val ? wl.val + (size_t)g0 * 32 + lane : nullptr;
-      // all slot blocks of a group in one or two batches (12 to 20 blocks at
-      // N = 65536): one index round trip, then one gather round trip
-      constexpr int NB = KC == 1 ? 16 : 8 / KC;
+      constexpr int NB = 8 / KC;  // 32 gathered operands in registers per batch
       int q = 0, qend = __shfl_sync(0xffffffffu, bnd, 1) - g0;  // chunk of block b
       for (int b = 0; b < nb; b += NB) {
         uint2 iv[NB];

@@ -34,7 +34,7 @@ namespace sdnn {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kAhead = 8;  // entries whose edges are in flight at once
+constexpr int kAhead = 16;  // entries whose edges are in flight at once
 
 __device__ __forceinline__ float clamp_hi(float v, float hi) { return fminf(hi, fmaxf(0.f, v)); }
 
