@@ -784,6 +784,16 @@ def run_serving(args, sg, local=0):
         for l, (ro, c, v) in enumerate(layers):
             e.set_layer_csr(l, ro, c, v)
         engines[mode] = e
+    # the SNICIT engine's settings come from the autotuner on a sample pass of
+    # the pool (threshold, centroids, sparse or dense residues, merging -- or
+    # no clustering at all); the server's slots take them over
+    rec = os.path.join(args.record_dir, "autotune_serve-mlp-1024x120.jsonl")
+    os.makedirs(os.path.dirname(rec), exist_ok=True)
+    if os.path.exists(rec):
+        os.remove(rec)
+    tuned = engines["SNICIT"].autotune(pool[:4096], rec)
+    out["snicit_settings"] = {k: tuned[k] for k in ("threshold", "centroid_candidates",
+                                                      "merge_start", "tile_rows", "threads")}
     arms = [("continuous_snicit", "SNICIT", dict(slots=2), arrivals),
             ("continuous_plain", "SNIG", dict(slots=2), arrivals),
             ("per_request_plain", "SNIG", dict(slots=1, max_requests_per_pass=1), arrivals),

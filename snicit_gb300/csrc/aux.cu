@@ -357,14 +357,26 @@ __global__ void assign_kernel(ClusterArgs a) {
     const int r = a.live[i];
     if (a.is_centroid[r]) continue;
     float* yr = a.y + (size_t)r * N;
+    const float4* yr4 = reinterpret_cast<const float4*>(yr);
     int best = INT_MAX, bk = 0;
     for (int k = 0; k < nc; ++k) {
-      const float* yc = a.y + (size_t)a.clist[k] * N;
-      int dl = 0, dt = 0;
+      const float4* yc4 = reinterpret_cast<const float4*>(a.y + (size_t)a.clist[k] * N);
+      int dt = 0;
+      // 1024 entries per step, all 16 loads of a lane in flight before the
+      // comparisons; stop as soon as this centroid cannot be nearer
       for (int j0 = 0; j0 < N; j0 += 1024) {
-        const int j1 = min(N, j0 + 1024);
-        for (int j = j0 + lane; j < j1; j += 32) dl += (yr[j] != yc[j]) ? 1 : 0;
-        dt = __reduce_add_sync(0xffffffffu, dl);
+        float4 u[8], v[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int j = j0 + 128 * t + 4 * lane;
+          u[t] = j < N ? yr4[j >> 2] : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[t] = j < N ? yc4[j >> 2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        int dl = 0;
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          dl += (u[t].x != v[t].x) + (u[t].y != v[t].y) + (u[t].z != v[t].z) + (u[t].w != v[t].w);
+        dt += (int)__reduce_add_sync(0xffffffffu, (unsigned)dl);
         if (dt >= best) break;
       }
       if (dt < best) {

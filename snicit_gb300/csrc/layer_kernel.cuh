@@ -77,10 +77,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 __device__ __forceinline__ float clampf(float v, float hi) { return fminf(hi, fmaxf(0.f, v)); }
-// Hint: bring `bytes` (a multiple of 16, 16-byte aligned source) into L2.
-__device__ __forceinline__ void prefetch_l2(const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
+
 
 // Applies NB blocks of slots (indices in iv, values in vv) to acc[T].
 template <int T, int RSW, bool CONSTW, int NB>
@@ -421,21 +418,6 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
         if (tid == 0) {
           load_tile(a, ys, RS, s_rows[0], nrows, q, &bar[0]);
           s_fail = mbar_wait_bounded(&bar[0], phase, a.err) ? 0 : 1;
-          // while the warps work on chunk q, bring the next chunk this CTA
-          // loads (chunk q + 1 of these rows, else chunk 0 of its next tile)
-          // into L2, so the next load does not wait on DRAM
-          if (!s_fail) {
-            if (q + 1 < a.nq) {
-              for (int t = 0; t < nrows; ++t)
-                prefetch_l2(a.y_in + (size_t)s_rows[0][t] * a.N + (size_t)(q + 1) * a.Q,
-                            (uint32_t)a.Q * 4u);
-            } else if (item + gridDim.x < sp.items) {
-              const int row1 = (int)((item + gridDim.x) / sp.spl) * T;
-              const int n1 = min(T, sp.count - row1);
-              for (int t = 0; t < n1; ++t)
-                prefetch_l2(a.y_in + (size_t)a.list_in[row1 + t] * a.N, (uint32_t)a.Q * 4u);
-            }
-          }
         }
         __syncthreads();
         if (s_fail) return;
