@@ -332,8 +332,10 @@ template <int T, int RSW, int KG, bool CONSTW>
 __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const LayerArgs a) {
   extern __shared__ __align__(128) float ys[];
   __shared__ __align__(8) uint64_t bar[1];
-  __shared__ int32_t s_rows[1][T];
-  __shared__ uint32_t s_mask;
+  __shared__ int32_t s_rows[2][T];
+  __shared__ int32_t s_next[T];
+  __shared__ uint32_t s_mask, s_pmask;
+  __shared__ int32_t s_ptile, s_pbuf;
   __shared__ int32_t s_fail;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -358,21 +360,43 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
   if (sp.count <= 0 || (long)blockIdx.x >= sp.items) return;
   __syncthreads();
 
-  if constexpr (KG == 1) {
-    // one buffer, whole rows (one chunk): reload per item, all groups of the part
-    uint32_t phase = 0;
-    int loaded_tile = -1;
-    for (long item = blockIdx.x; item < sp.items; item += gridDim.x) {
-      const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
-      const int row0 = tile * T;
-      const int nrows = min(T, sp.count - row0);
-      const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
-      __syncthreads();
-      if (tid < T) s_rows[0][tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
-      __syncthreads();
+  // Per item: row ids of the item after it are fetched while it runs, and the
+  // rows it flags are published (tile mask, ticket, list append: a chain of
+  // global atomics) during the next item, while the other warps already work
+  // on it -- both by the CTA's last warp (its lane 31 publishes); s_rows is
+  // double-buffered, and the pending state lives in shared memory so that it
+  // costs the compute warps no registers.
+  const bool last_warp = warp == nwarps - 1;
+  auto item_row = [&](long it, int t) -> int {
+    const int r0 = (int)(it / sp.spl) * T;
+    return t < min(T, sp.count - r0) ? a.list_in[r0 + t] : -1;
+  };
+  if (last_warp && lane < T) s_next[lane] = item_row(blockIdx.x, lane);
+  if (last_warp && lane == 31) s_ptile = -1;
+  uint32_t phase = 0;
+  int loaded_tile = -1;
+  int b = 0;
+  for (long item = blockIdx.x; item < sp.items; item += gridDim.x, b ^= 1) {
+    const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
+    const int row0 = tile * T;
+    const int nrows = min(T, sp.count - row0);
+    const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
+    __syncthreads();  // s_rows[b] is free: the item that used it was published
+    if (tid < T) s_rows[b][tid] = s_next[tid];
+    __syncthreads();
+    if (last_warp) {
+      if (lane < T && item + gridDim.x < sp.items) s_next[lane] = item_row(item + gridDim.x, lane);
+      if (lane == 31 && s_ptile >= 0) {
+        publish_rows<T>(a, s_pmask, s_ptile, sp.spl, s_rows[s_pbuf]);
+        s_ptile = -1;
+      }
+    }
+    uint32_t m = 0;
+    if constexpr (KG == 1) {
+      // one buffer, whole rows (one chunk): reloaded when the tile changes
       if (tile != loaded_tile) {
         if (tid == 0) {
-          load_tile(a, ys, RS, s_rows[0], nrows, 0, &bar[0]);
+          load_tile(a, ys, RS, s_rows[b], nrows, 0, &bar[0]);
           s_fail = mbar_wait_bounded(&bar[0], phase, a.err) ? 0 : 1;
         }
         __syncthreads();
@@ -381,33 +405,15 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
         phase ^= 1u;
         loaded_tile = tile;
       }
-      uint32_t m = 0;
       for (int g = gbeg + warp; g < gend; g += nwarps) {
         float acc[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) acc[t] = 0.f;
         accumulate_group<T, RSW, CONSTW>(acc, a.w, a.nq, ys, RS, g, 0, lane);
-        m |= epilogue_group<T>(acc, a, s_rows[0], nrows, g, lane);
+        m |= epilogue_group<T>(acc, a, s_rows[b], nrows, g, lane);
       }
-      if (lane == 0 && m) atomicOr(&s_mask, m);
-      __syncthreads();
-      if (tid == 0) {
-        const uint32_t mm = s_mask;
-        s_mask = 0;
-        publish_rows<T>(a, mm, tile, sp.spl, s_rows[0]);
-      }
-    }
-  } else {
-    // input chunks (nq > 1): accumulators of KG groups per warp live across chunks
-    uint32_t phase = 0;
-    for (long item = blockIdx.x; item < sp.items; item += gridDim.x) {
-      const int tile = (int)(item / sp.spl), part = (int)(item % sp.spl);
-      const int row0 = tile * T;
-      const int nrows = min(T, sp.count - row0);
-      const int gbeg = (int)((long)a.G * part / sp.spl), gend = (int)((long)a.G * (part + 1) / sp.spl);
-      __syncthreads();
-      if (tid < T) s_rows[0][tid] = tid < nrows ? a.list_in[row0 + tid] : -1;
-      __syncthreads();
+    } else {
+      // input chunks (nq > 1): accumulators of KG groups per warp live across chunks
       float acc[KG][T];
 #pragma unroll
       for (int kk = 0; kk < KG; ++kk)
@@ -416,7 +422,7 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
       for (int q = 0; q < a.nq; ++q) {
         if (q > 0) __syncthreads();
         if (tid == 0) {
-          load_tile(a, ys, RS, s_rows[0], nrows, q, &bar[0]);
+          load_tile(a, ys, RS, s_rows[b], nrows, q, &bar[0]);
           s_fail = mbar_wait_bounded(&bar[0], phase, a.err) ? 0 : 1;
         }
         __syncthreads();
@@ -426,21 +432,23 @@ __global__ void __launch_bounds__(KG <= 8 ? 1024 : 512) layer_kernel(const Layer
         accumulate_chunk<T, RSW, CONSTW, KG>(acc, a.w, a.nq, ys, RS, gbeg, gend, warp, nwarps, q,
                                              lane);
       }
-      uint32_t m = 0;
 #pragma unroll
       for (int kk = 0; kk < KG; ++kk) {
         const int g = gbeg + warp + kk * nwarps;
-        if (g < gend) m |= epilogue_group<T>(acc[kk], a, s_rows[0], nrows, g, lane);
-      }
-      if (lane == 0 && m) atomicOr(&s_mask, m);
-      __syncthreads();
-      if (tid == 0) {
-        const uint32_t mm = s_mask;
-        s_mask = 0;
-        publish_rows<T>(a, mm, tile, sp.spl, s_rows[0]);
+        if (g < gend) m |= epilogue_group<T>(acc[kk], a, s_rows[b], nrows, g, lane);
       }
     }
+    if (lane == 0 && m) atomicOr(&s_mask, m);
+    __syncthreads();
+    if (last_warp && lane == 31) {
+      s_pmask = s_mask;
+      s_mask = 0;
+      s_ptile = tile;
+      s_pbuf = b;
+    }
   }
+  if (last_warp && lane == 31 && s_ptile >= 0)
+    publish_rows<T>(a, s_pmask, s_ptile, sp.spl, s_rows[s_pbuf]);
 }
 
 #define SDNN_LAYER_INSTANCE(T, RSW, KG, CW) template __global__ void layer_kernel<T, RSW, KG, CW>(const LayerArgs);
