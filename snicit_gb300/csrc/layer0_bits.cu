@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(256, 3) layer0_bits_kernel(const Layer0Args a)
 // epilogue is the one of layer0_bits_kernel.  The rows that survive are
 // published per tile through the tile mask and ticket (the last subset of a
 // tile to finish appends them).
-constexpr int kChunkGroupsPerWarp = 8;
+constexpr int kChunkGroupsPerWarp = 4;
 constexpr int kChunkWarps = 16;
 
 __global__ void __launch_bounds__(256) bits_transpose_kernel(const Layer0Args a) {
