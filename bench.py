@@ -833,8 +833,8 @@ def run_case(args):
                     merge_start=args.merge_start, merge_every=args.merge_every,
                     merge=not args.case.startswith("residue"),
                     # ncu cannot profile kernels inside a graph with a conditional
-                    # node: the residue cases let the host choose the post path
-                    device_post_choice=not args.case.startswith("residue"),
+                    # node: the cases let the host choose the post path
+                    device_post_choice=False,
                     sparse_residue=not args.dense_residue)
     eng.generate_weights(SEED, NNZ, 0.0625)
     for _ in range(2):
