@@ -507,12 +507,16 @@ typedef struct {
   int N, L, nnz, ngroups, nthreads;
   uint64_t seed;
   float wval, bias, clampv;
-  float* y;                 /* rows * N, updated in place */
+  float* ybuf[2];           /* rows * N each: layer l reads ybuf[l & 1], writes the other */
   int64_t rows;
   const int64_t* group_off; /* ngroups + 1 row offsets */
-  int32_t* live;            /* rows */
-  int32_t* cols;            /* N * nnz of the current layer */
-  int layer;
+  int32_t* live;            /* rows: alive before the current layer */
+  int32_t* live_next;       /* rows: some output > 0 in the current layer */
+  int32_t* cols;            /* N * nnz out-edges of the current layer, by input */
+  int32_t* tin_off;         /* N + 1: in-edges of every output ... */
+  int32_t* tin;             /* N * nnz ... inputs ascending */
+  int64_t* tot;             /* nthreads: edges per thread's output range */
+  int32_t* cnt;             /* nthreads * N: per-thread edge counts, then positions */
   int64_t next;             /* work counter of the current phase */
   double* secs;             /* ngroups */
   pthread_barrier_t bar;
@@ -523,51 +527,95 @@ typedef struct {
   int t;
 } stream_arg;
 
+enum { kPortBlock = 4096 };  /* outputs per work item */
+
 static void* stream_worker(void* p) {
   stream_arg* a = (stream_arg*)p;
   stream_job* j = a->j;
   const int N = j->N, nnz = j->nnz, T = j->nthreads;
-  float* acc = (float*)malloc(sizeof(float) * (size_t)N);
+  const int c0 = (int)((int64_t)N * a->t / T), c1 = (int)((int64_t)N * (a->t + 1) / T);
+  const int nblk = (N + kPortBlock - 1) / kPortBlock;
   for (int l = 0; l < j->L; ++l) {
-    /* weights of layer l: input rows split over the threads (untimed) */
+    const float* yin_all = j->ybuf[l & 1];
+    float* yout_all = j->ybuf[(l + 1) & 1];
+    /* weights of layer l: input rows split over the threads, then the
+       in-edges of every output (inputs ascending), outputs split over the
+       threads (untimed) */
     for (int i = (int)((int64_t)N * a->t / T); i < (int)((int64_t)N * (a->t + 1) / T); ++i)
       gen_row_cols(j->seed, l, i, N, nnz, j->cols + (int64_t)i * nnz);
     pthread_barrier_wait(&j->bar);
+    {
+      /* in-edges by output, inputs ascending: thread t counts the edges of its
+         input range per output (cnt row t), the output ranges turn the counts
+         into positions (outputs in order, then threads in order, so that the
+         inputs of an output stay ascending), and each thread places its edges */
+      const int i0 = (int)((int64_t)N * a->t / T), i1 = (int)((int64_t)N * (a->t + 1) / T);
+      int32_t* mycnt = j->cnt + (int64_t)a->t * N;
+      memset(mycnt, 0, sizeof(int32_t) * (size_t)N);
+      for (int64_t e = (int64_t)i0 * nnz; e < (int64_t)i1 * nnz; ++e) mycnt[j->cols[e]]++;
+      pthread_barrier_wait(&j->bar);
+      int64_t mine = 0;
+      for (int c = c0; c < c1; ++c)
+        for (int t = 0; t < T; ++t) mine += j->cnt[(int64_t)t * N + c];
+      j->tot[a->t] = mine;
+      pthread_barrier_wait(&j->bar);
+      int64_t run = 0;
+      for (int t = 0; t < a->t; ++t) run += j->tot[t];
+      for (int c = c0; c < c1; ++c) {
+        j->tin_off[c] = (int32_t)run;
+        for (int t = 0; t < T; ++t) {
+          const int32_t n = j->cnt[(int64_t)t * N + c];
+          j->cnt[(int64_t)t * N + c] = (int32_t)run;  /* thread t's first position for c */
+          run += n;
+        }
+      }
+      if (a->t == T - 1) j->tin_off[N] = (int32_t)run;
+      pthread_barrier_wait(&j->bar);
+      for (int i = i0; i < i1; ++i)
+        for (int k = 0; k < nnz; ++k) j->tin[mycnt[j->cols[(int64_t)i * nnz + k]]++] = i;
+    }
+    for (int64_t r = (j->rows * a->t) / T; r < (j->rows * (a->t + 1)) / T; ++r) j->live_next[r] = 0;
+    pthread_barrier_wait(&j->bar);
     for (int g = 0; g < j->ngroups; ++g) {
       double t0 = 0.0;
+      const int64_t g0 = j->group_off[g], items = (j->group_off[g + 1] - g0) * nblk;
       if (a->t == 0) {
-        __atomic_store_n(&j->next, j->group_off[g], __ATOMIC_SEQ_CST);
+        __atomic_store_n(&j->next, 0, __ATOMIC_SEQ_CST);
         t0 = now_s();
       }
       pthread_barrier_wait(&j->bar);
       for (;;) {
-        const int64_t r = __atomic_fetch_add(&j->next, 1, __ATOMIC_SEQ_CST);
-        if (r >= j->group_off[g + 1]) break;
+        const int64_t it = __atomic_fetch_add(&j->next, 1, __ATOMIC_SEQ_CST);
+        if (it >= items) break;
+        const int64_t r = g0 + it / nblk;
         if (!j->live[r]) continue;
-        float* y = j->y + r * (int64_t)N;
-        memset(acc, 0, sizeof(float) * (size_t)N);
-        for (int i = 0; i < N; ++i) {
-          const float v = y[i];
-          if (v == 0.f) continue;
-          const int32_t* co = j->cols + (int64_t)i * nnz;
-          for (int k = 0; k < nnz; ++k) {
-            const float prod = v * j->wval;
-            acc[co[k]] = acc[co[k]] + prod;
-          }
-        }
+        const int b0 = (int)(it % nblk) * kPortBlock, b1 = b0 + kPortBlock < N ? b0 + kPortBlock : N;
+        const float* y = yin_all + r * (int64_t)N;
+        float* yo = yout_all + r * (int64_t)N;
         int any = 0;
-        for (int c = 0; c < N; ++c) {
-          const float v = acc[c] + j->bias;
+        /* each output sums its nonzero inputs in ascending order, products
+           first: the arithmetic of the input-major scatter of oracle_infer */
+        for (int c = b0; c < b1; ++c) {
+          float acc = 0.f;
+          for (int32_t e = j->tin_off[c]; e < j->tin_off[c + 1]; ++e) {
+            const float v = y[j->tin[e]];
+            if (v == 0.f) continue;
+            const float prod = v * j->wval;
+            acc = acc + prod;
+          }
+          const float v = acc + j->bias;
           if (v > 0.f) any = 1;
-          y[c] = v < 0.f ? 0.f : (v > j->clampv ? j->clampv : v);
+          yo[c] = v < 0.f ? 0.f : (v > j->clampv ? j->clampv : v);
         }
-        if (!any) j->live[r] = 0;
+        if (any) __atomic_store_n(&j->live_next[r], 1, __ATOMIC_RELAXED);
       }
       pthread_barrier_wait(&j->bar);
       if (a->t == 0) j->secs[g] += now_s() - t0;
     }
+    for (int64_t r = (j->rows * a->t) / T; r < (j->rows * (a->t + 1)) / T; ++r)
+      j->live[r] = j->live[r] && j->live_next[r];
+    pthread_barrier_wait(&j->bar);
   }
-  free(acc);
   return NULL;
 }
 
@@ -576,8 +624,9 @@ static void* stream_worker(void* p) {
  * scalar bias) over the rows of Y (rows x N, overwritten with the final
  * activations).  Rows [group_off[g], group_off[g+1]) form group g; secs[g]
  * receives the wall time of group g's layer arithmetic summed over the
- * layers (all threads on one group at a time).  alive_out[r] = 1 if row r
- * survives every layer. */
+ * layers (all threads on one group at a time: a work item is a row's block of
+ * 4096 outputs, so the threads stay busy when only a few rows are left alive).
+ * alive_out[r] = 1 if row r survives every layer. */
 int oracle_port_stream(int N, int L, uint64_t seed, int nnz, float wval, float bias, float clampv,
                        float* Y, int64_t rows, const int64_t* group_off, int ngroups,
                        int nthreads, int32_t* alive_out, double* secs) {
@@ -596,12 +645,19 @@ int oracle_port_stream(int N, int L, uint64_t seed, int nnz, float wval, float b
   j.wval = wval;
   j.bias = bias;
   j.clampv = clampv;
-  j.y = Y;
   j.rows = rows;
   j.group_off = group_off;
   j.secs = secs;
+  const size_t ysz = sizeof(float) * (size_t)(rows > 0 ? rows : 1) * (size_t)N;
+  j.ybuf[0] = Y;
+  j.ybuf[1] = (float*)malloc(ysz);
   j.live = (int32_t*)malloc(sizeof(int32_t) * (size_t)(rows > 0 ? rows : 1));
+  j.live_next = (int32_t*)malloc(sizeof(int32_t) * (size_t)(rows > 0 ? rows : 1));
   j.cols = (int32_t*)malloc(sizeof(int32_t) * (size_t)N * (size_t)nnz);
+  j.tin = (int32_t*)malloc(sizeof(int32_t) * (size_t)N * (size_t)nnz);
+  j.tin_off = (int32_t*)malloc(sizeof(int32_t) * (size_t)(N + 1));
+  j.tot = (int64_t*)calloc((size_t)nthreads, sizeof(int64_t));
+  j.cnt = (int32_t*)malloc(sizeof(int32_t) * (size_t)nthreads * (size_t)N);
   /* every row enters layer 0 (an all-zero row dies there, BF.hpp:222-229) */
   for (int64_t r = 0; r < rows; ++r) j.live[r] = 1;
   for (int g = 0; g < ngroups; ++g) secs[g] = 0.0;
@@ -616,14 +672,22 @@ int oracle_port_stream(int N, int L, uint64_t seed, int nnz, float wval, float b
   stream_worker(&args[0]);
   for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
   pthread_barrier_destroy(&j.bar);
+  const float* fin = j.ybuf[L & 1];
   for (int64_t r = 0; r < rows; ++r) {
     if (alive_out) alive_out[r] = j.live[r];
     if (!j.live[r]) memset(Y + r * (int64_t)N, 0, sizeof(float) * (size_t)N);
+    else if (fin != Y) memcpy(Y + r * (int64_t)N, fin + r * (int64_t)N, sizeof(float) * (size_t)N);
   }
   free(th);
   free(args);
+  free(j.ybuf[1]);
   free(j.live);
+  free(j.live_next);
   free(j.cols);
+  free(j.tin);
+  free(j.tin_off);
+  free(j.tot);
+  free(j.cnt);
   return 0;
 }
 
