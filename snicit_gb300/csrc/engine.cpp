@@ -50,7 +50,6 @@ struct DevLayer {
   int64_t slots = 0;
   int32_t max_depth = 0;
   uint32_t chain_slice8 = 0, chain_slice16 = 0;  // largest per-CTA weight slices (chain)
-  uint32_t grid_slice = 0;  // largest per-CTA slot-index range of the grid chain
 };
 
 struct GraphKey {
@@ -221,7 +220,6 @@ struct sdnn_engine {
   int chain_kc = 1;
   int chain_kind = 0;           // 1 cluster chain kernel, 2 grid chain kernel
   uint32_t chain_wcap8 = 0, chain_wcap16 = 0;  // chain kernel weight slices (bytes)
-  uint32_t grid_wcap = 0;  // grid chain: staging buffer bytes (0 = indices from global)
   bool last_chain = false;
   int last_post_kernel = 0;     // stats: 0 none, 1 per-layer launches, 2/3 chain kernel 1/2
   LayerDev* d_layer_table = nullptr;  // device copy of every layer's descriptor
@@ -629,7 +627,6 @@ int upload_layer(sdnn_engine* e, int l, const PackedView& p, std::string& err) {
     d.chain_slice8 = chain_slice_bytes(p.grp_blk, e->G, !p.constw, 8);
     d.chain_slice16 = chain_slice_bytes(p.grp_blk, e->G, !p.constw, 16);
   }
-  if (e->num_sms > 0) d.grid_slice = grid_chain_slice_bytes(p.grp_blk, e->G, e->nq, e->num_sms);
   const size_t nslot = (size_t)p.nblocks * 128;
   const size_t ngrp = (size_t)e->G * e->nq + 1;
   cudaError_t rc = cudaSuccess;
@@ -864,14 +861,10 @@ int finalize_weights(sdnn_engine* e) {
   }
   e->chain_cap = e->nq == 1 ? chain_capacity(e->N) : 0;
   e->chain_wcap8 = e->chain_wcap16 = 0;
-  e->grid_wcap = 0;
   for (const DevLayer& d : e->dl) {
     e->chain_wcap8 = std::max(e->chain_wcap8, d.chain_slice8);
     e->chain_wcap16 = std::max(e->chain_wcap16, d.chain_slice16);
-    e->grid_wcap = std::max(e->grid_wcap, d.grid_slice);
   }
-  // two staging buffers must fit shared memory next to the kernel's own
-  if (e->grid_wcap > 100u * 1024u) e->grid_wcap = 0;
   if (!e->pos.empty()) {
     CK(cudaMalloc((void**)&e->d_perm_final, (size_t)e->N * 4));
     CK(cudaMemcpy(e->d_perm_final, e->pos[e->L - 1].data(), (size_t)e->N * 4,
@@ -1205,7 +1198,6 @@ int enqueue(sdnn_engine* e, int phase, int64_t rows, const float* d_in, int32_t*
     ga.scratch = e->d_gscratch;
     ga.barrier = e->d_gbar;
     ga.err = e->d_err;
-    ga.wcap = e->grid_wcap;
     CK(launch_grid_chain(ga, e->chain_kc, e->num_sms, s));
     e->launches++;
     if ((rc = record(e, 3, capturing))) return rc;
@@ -2397,7 +2389,6 @@ int engine_share_weights(sdnn_engine* dst, sdnn_engine* src) {
   dst->chain_cap = src->chain_cap;
   dst->chain_wcap8 = src->chain_wcap8;
   dst->chain_wcap16 = src->chain_wcap16;
-  dst->grid_wcap = src->grid_wcap;
   dst->weights_owner = src;
   dst->weights_dirty = false;
   src->share_users.fetch_add(1);

@@ -15,8 +15,6 @@
 //  * a grid barrier (one counter, bounded wait) separates layers; the last
 //    layer writes the rows to the final activation buffer.
 // Bitwise equal to the per-layer launches.
-#include <algorithm>
-
 #include "layer_kernel.cuh"
 
 namespace sdnn {
@@ -53,82 +51,10 @@ __device__ __forceinline__ void grid_barrier(unsigned int* ctr, unsigned int tar
   __syncthreads();
 }
 
-// One output group of one layer: its slot blocks (all chunks, consecutive:
-// chunk-major, the layer kernel's order) in batches of NB blocks -- all index
-// loads, then all gathers, then the FMAs -- with the chunk boundaries
-// (nq + 1 offsets, nq <= 31) held by the lanes.  `ip` points at the group's
-// first block for this lane, in global or (staged) shared memory.
-template <int KC>
-__device__ __forceinline__ void grid_group(const GridChainArgs& a, const LayerDev& wl, int g, int K,
-                                           const uint2* ip, const float* in, float* out,
-                                           bool last, int lane, size_t cs, size_t rs, bool bytes) {
-  const int nq = a.nq, Q = a.Q, N = a.N;
-  const int c = g * 32 + lane;
-  const float bc = wl.bias_vec ? __ldg(wl.bias_vec + c) : wl.bias;
-  float acc[KC];
-#pragma unroll
-  for (int t = 0; t < KC; ++t) acc[t] = 0.f;
-  const int32_t bnd = lane <= nq ? __ldg(wl.grp_blk + g * nq + lane) : 0;
-  const int32_t g0 = __shfl_sync(0xffffffffu, bnd, 0);
-  const int nb = __shfl_sync(0xffffffffu, bnd, nq) - g0;
-  const float4* vp = wl.val ? wl.val + (size_t)g0 * 32 + lane : nullptr;
-  constexpr int NB = 8 / KC;  // 32 gathered operands in registers per batch
-  int q = 0, qend = __shfl_sync(0xffffffffu, bnd, 1) - g0;  // chunk of block b
-  for (int b = 0; b < nb; b += NB) {
-    uint2 iv[NB];
-#pragma unroll
-    for (int k = 0; k < NB; ++k) iv[k] = b + k < nb ? ip[(size_t)(b + k) * 32] : make_uint2(0u, 0u);
-    float y[NB][4][KC];
-#pragma unroll
-    for (int k = 0; k < NB; ++k) {
-      while (b + k >= qend && q + 1 < nq) {  // warp-uniform: next chunk
-        ++q;
-        qend = __shfl_sync(0xffffffffu, bnd, q + 1) - g0;
-      }
-      const float* base = in + (size_t)q * cs;
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {
-        uint32_t j = ((s < 2 ? iv[k].x : iv[k].y) >> ((s & 1) * 16)) & 0xffffu;
-        if (bytes) j >>= 2;
-#pragma unroll
-        for (int t = 0; t < KC; ++t) y[k][s][t] = (t < K && b + k < nb) ? base[(size_t)t * rs + j] : 0.f;
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < NB; ++k) {
-      if (b + k < nb) {
-        float4 wv = make_float4(wl.wconst, wl.wconst, wl.wconst, wl.wconst);
-        if (vp) wv = __ldg(vp + (size_t)(b + k) * 32);
-        const float w4[4] = {wv.x, wv.y, wv.z, wv.w};
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-#pragma unroll
-          for (int t = 0; t < KC; ++t) acc[t] = fmaf(w4[s], y[k][s][t], acc[t]);
-      }
-    }
-  }
-#pragma unroll
-  for (int t = 0; t < KC; ++t) {
-    if (t < K) {
-      const float yv = clampf(acc[t] + bc, a.clampv);
-      if (last)
-        a.y_out[(size_t)a.clist[t] * N + c] = yv;
-      else
-        out[(size_t)t * rs + (size_t)(c / Q) * cs + (c % Q)] = yv;
-    }
-  }
-}
-
-// The groups of CTA c: [c * gpc, min(G, (c + 1) * gpc)) with gpc = ceil(G / grid);
-// consecutive groups have consecutive slot blocks.
-__host__ __device__ inline int grid_groups_per_cta(int G, int grid) { return (G + grid - 1) / grid; }
-
 template <int KC>
 __global__ void __launch_bounds__(kGridChainThreads) chain_grid_kernel(const GridChainArgs a) {
-  extern __shared__ __align__(128) uint2 sidx[];  // staged slot blocks: 2 x wcap bytes
   __shared__ int32_t s_failed;
-  __shared__ __align__(8) uint64_t sbar[2];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, wpc = blockDim.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31;
   const int N = a.N, Q = a.Q, nq = a.nq;
   const int K = min(*a.ccount, KC);
   const size_t cs = (size_t)Q + 32;        // chunk stride in the scratch rows
@@ -137,39 +63,7 @@ __global__ void __launch_bounds__(kGridChainThreads) chain_grid_kernel(const Gri
   const long gthreads = (long)gridDim.x * blockDim.x;
   const int gwarp = (int)(gtid >> 5), nwarps = (int)(gthreads >> 5);
   const bool bytes = slot_index_in_bytes(Q);
-  const bool staged = a.wcap > 0;
-  const int gpc = grid_groups_per_cta(a.G, gridDim.x);
-  const int cg0 = min(a.G, (int)blockIdx.x * gpc), cg1 = min(a.G, cg0 + gpc);
-  const uint32_t wcap_blocks = a.wcap / 256u;  // 32 lanes x 8 B per block
-  // Staged mode: this CTA's slot blocks of layer l sit in buffer l & 1; thread
-  // 0 copies those of layer l + 1 (one bulk copy, one layer ahead) while layer
-  // l runs.  Buffer (l + 1) & 1 last held layer l - 1, which every warp of the
-  // CTA finished before the grid barrier that opens layer l.
-  auto stage = [&](int l, int buf) {
-    const LayerDev wn = a.layers[l];
-    const int32_t b0 = __ldg(wn.grp_blk + cg0 * nq), b1 = __ldg(wn.grp_blk + cg1 * nq);
-    uint32_t n = (uint32_t)(b1 - b0) * 256u;
-    if (n > a.wcap) {  // cannot happen with the host's wcap; recorded, not copied
-      atomicExch(a.err, DEV_BAD_ROW);
-      n = 0;
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(&sbar[buf], n);
-    const char* src = reinterpret_cast<const char*>(wn.idx + (size_t)b0 * 32);
-    char* dst = reinterpret_cast<char*>(sidx + (size_t)buf * wcap_blocks * 32);
-    for (uint32_t off = 0; off < n; off += 32768u)
-      bulk_g2s(dst + off, src + off, min(32768u, n - off), &sbar[buf]);
-  };
-  uint32_t sphase[2] = {0u, 0u};
-  if (tid == 0) {
-    s_failed = 0;
-    if (staged) {
-      mbar_init(&sbar[0], 1);
-      mbar_init(&sbar[1], 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      stage(a.first, 0);
-    }
-  }
+  if (tid == 0) s_failed = 0;
   unsigned int arrivals = 0;
   const int nbuf = a.last - a.first;  // buffers 0 .. nbuf - 1 (the last layer writes y_out)
   // rows into buffer 0, pad columns of every buffer zeroed
@@ -190,57 +84,91 @@ __global__ void __launch_bounds__(kGridChainThreads) chain_grid_kernel(const Gri
     float* out = a.scratch + (size_t)(li + 1) * KC * rs;
     const bool last = l + 1 == a.last;
     const LayerDev wl = a.layers[l];
-    if (staged) {
-      const int buf = li & 1;
-      if (tid == 0) {
-        if (l + 1 < a.last) stage(l + 1, buf ^ 1);
-        if (!s_failed && !mbar_wait_bounded(&sbar[buf], sphase[buf], a.err)) s_failed = 1;
+    if (tid == 0 && l + 1 < a.last) {
+      // this CTA's slot blocks of the next layer into L2 while this one runs
+      const int gb = blockIdx.x * (blockDim.x >> 5);
+      const int ge = min(a.G, gb + (int)(blockDim.x >> 5));
+      if (gb < ge) {
+        const LayerDev wn = a.layers[l + 1];
+        const int32_t b0 = __ldg(wn.grp_blk + gb * nq), b1 = __ldg(wn.grp_blk + ge * nq);
+        const uint32_t bytes = (uint32_t)(b1 - b0) * 32u * (uint32_t)sizeof(uint2);
+        if (bytes > 0)
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wn.idx + (size_t)b0 * 32),
+                       "r"(bytes)
+                       : "memory");
+        if (wn.val && bytes > 0)
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wn.val + (size_t)b0 * 32),
+                       "r"(bytes * 2u)
+                       : "memory");
       }
-      __syncthreads();
-      mbar_try_wait(&sbar[buf], sphase[buf]);
-      sphase[buf] ^= 1u;
-      if (!s_failed) {
-        const int32_t cb0 = __ldg(wl.grp_blk + cg0 * nq);
-        const uint2* sb = sidx + (size_t)buf * wcap_blocks * 32;
-        for (int g = cg0 + warp; g < cg1; g += wpc) {
-          const int32_t gb = __ldg(wl.grp_blk + g * nq);
-          grid_group<KC>(a, wl, g, K, sb + (size_t)(gb - cb0) * 32 + lane, in, out, last, lane,
-                         cs, rs, bytes);
+    }
+    for (int g = gwarp; g < a.G; g += nwarps) {
+      const int c = g * 32 + lane;
+      const float bc = wl.bias_vec ? __ldg(wl.bias_vec + c) : wl.bias;
+      float acc[KC];
+#pragma unroll
+      for (int t = 0; t < KC; ++t) acc[t] = 0.f;
+      // the group's slot blocks of all chunks are consecutive: walk them as one
+      // sequence (chunk-major, the layer kernel's order) in batches of NB
+      // blocks -- all index loads, then all gathers, then the FMAs -- with the
+      // chunk boundaries (nq + 1 offsets, nq <= 31) held by the lanes
+      const int32_t bnd = lane <= nq ? __ldg(wl.grp_blk + g * nq + lane) : 0;
+      const int32_t g0 = __shfl_sync(0xffffffffu, bnd, 0);
+      const int nb = __shfl_sync(0xffffffffu, bnd, nq) - g0;
+      const uint2* ip = wl.idx + (size_t)g0 * 32 + lane;
+      const float4* vp = wl.val ? wl.val + (size_t)g0 * 32 + lane : nullptr;
+      constexpr int NB = 8 / KC;  // 32 gathered operands in registers per batch
+      int q = 0, qend = __shfl_sync(0xffffffffu, bnd, 1) - g0;  // chunk of block b
+      for (int b = 0; b < nb; b += NB) {
+        uint2 iv[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k)
+          iv[k] = b + k < nb ? __ldg(ip + (size_t)(b + k) * 32) : make_uint2(0u, 0u);
+        float y[NB][4][KC];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+          while (b + k >= qend && q + 1 < nq) {  // warp-uniform: next chunk
+            ++q;
+            qend = __shfl_sync(0xffffffffu, bnd, q + 1) - g0;
+          }
+          const float* base = in + (size_t)q * cs;
+#pragma unroll
+          for (int s = 0; s < 4; ++s) {
+            uint32_t j = ((s < 2 ? iv[k].x : iv[k].y) >> ((s & 1) * 16)) & 0xffffu;
+            if (bytes) j >>= 2;
+#pragma unroll
+            for (int t = 0; t < KC; ++t)
+              y[k][s][t] = (t < K && b + k < nb) ? base[(size_t)t * rs + j] : 0.f;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+          if (b + k < nb) {
+            float4 wv = make_float4(wl.wconst, wl.wconst, wl.wconst, wl.wconst);
+            if (vp) wv = __ldg(vp + (size_t)(b + k) * 32);
+            const float w4[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+#pragma unroll
+              for (int t = 0; t < KC; ++t) acc[t] = fmaf(w4[s], y[k][s][t], acc[t]);
+          }
         }
       }
-    } else {
-      if (tid == 0 && l + 1 < a.last) {
-        // this CTA's slot blocks of the next layer into L2 while this one runs
-        const int gb = blockIdx.x * wpc;
-        const int ge = min(a.G, gb + wpc);
-        if (gb < ge) {
-          const LayerDev wn = a.layers[l + 1];
-          const int32_t b0 = __ldg(wn.grp_blk + gb * nq), b1 = __ldg(wn.grp_blk + ge * nq);
-          const uint32_t nbytes = (uint32_t)(b1 - b0) * 32u * (uint32_t)sizeof(uint2);
-          if (nbytes > 0)
-            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wn.idx + (size_t)b0 * 32),
-                         "r"(nbytes)
-                         : "memory");
-          if (wn.val && nbytes > 0)
-            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(wn.val + (size_t)b0 * 32),
-                         "r"(nbytes * 2u)
-                         : "memory");
+#pragma unroll
+      for (int t = 0; t < KC; ++t) {
+        if (t < K) {
+          const float y = clampf(acc[t] + bc, a.clampv);
+          if (last)
+            a.y_out[(size_t)a.clist[t] * N + c] = y;
+          else
+            out[(size_t)t * rs + (size_t)(c / Q) * cs + (c % Q)] = y;
         }
-      }
-      for (int g = gwarp; g < a.G; g += nwarps) {
-        const int32_t gb = __ldg(wl.grp_blk + g * nq);
-        grid_group<KC>(a, wl, g, K, wl.idx + (size_t)gb * 32 + lane, in, out, last, lane, cs, rs,
-                       bytes);
       }
     }
     if (!last) {
       arrivals += gridDim.x;
       grid_barrier(a.barrier, arrivals, a.err, &s_failed);
     }
-  }
-  if (staged && tid == 0 && s_failed) {
-    // a wait gave up: let this CTA's copies in flight land before it exits
-    for (int b = 0; b < 2; ++b) mbar_wait_bounded(&sbar[b], sphase[b], a.err, 100000000ull);
   }
 }
 
@@ -267,38 +195,23 @@ size_t grid_chain_scratch_floats(int layers, int nq, int Q) {
   return (size_t)(layers + 1) * grid_chain_capacity() * nq * ((size_t)Q + 32);
 }
 
-uint32_t grid_chain_slice_bytes(const int32_t* grp_blk, int G, int nq, int grid) {
-  const int gpc = grid_groups_per_cta(G, grid);
-  uint32_t mx = 0;
-  for (int c = 0; c < grid; ++c) {
-    const int g0 = std::min(G, c * gpc), g1 = std::min(G, g0 + gpc);
-    mx = std::max(mx, (uint32_t)(grp_blk[(size_t)g1 * nq] - grp_blk[(size_t)g0 * nq]) * 256u);
-  }
-  return mx;
-}
-
 cudaError_t launch_grid_chain(const GridChainArgs& a, int kc_needed, int num_sms, cudaStream_t s) {
   int kc = 1;
   while (kc < kc_needed) kc *= 2;
   const void* fn = grid_fn(kc);
   if (!fn || a.nq > 31) return cudaErrorInvalidValue;  // lanes hold the nq + 1 chunk offsets
-  // staged slot blocks: two buffers of wcap bytes (0: indices read from global)
-  const size_t smem = 2 * (size_t)a.wcap;
-  cudaError_t rc = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (rc != cudaSuccess) return rc;
   int per_sm = 0;
-  rc = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGridChainThreads, smem);
+  cudaError_t rc = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGridChainThreads, 0);
   if (rc != cudaSuccess) return rc;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  // every CTA must be resident at once (cooperative launch): one per SM; the
-  // host sized wcap for this grid (grid_chain_slice_bytes)
+  // every CTA must be resident at once (cooperative launch): one per SM
   const int grid = num_sms;
   rc = cudaMemsetAsync(a.barrier, 0, sizeof(unsigned int), s);
   if (rc != cudaSuccess) return rc;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kGridChainThreads);
-  cfg.dynamicSmemBytes = smem;
+  cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

@@ -155,14 +155,9 @@ struct GridChainArgs {
   float* scratch;            // [layers + 1][8][nq][Q + 32]: one buffer per layer
   unsigned int* barrier;     // grid barrier counter (zeroed by the launch)
   int32_t* err;
-  uint32_t wcap;             // bytes of one staging buffer for a CTA's slot indices of a
-                             // layer (two buffers, one layer ahead); 0 = read from global
 };
 int grid_chain_capacity();
 size_t grid_chain_scratch_floats(int layers, int nq, int Q);
-// Largest slot-index range (bytes) one CTA of a `grid`-CTA grid chain reads in
-// a layer (grp_blk: G * nq + 1 block offsets).
-uint32_t grid_chain_slice_bytes(const int32_t* grp_blk, int G, int nq, int grid);
 cudaError_t launch_grid_chain(const GridChainArgs& a, int kc_needed, int num_sms, cudaStream_t s);
 
 // ---- auxiliary kernels (aux.cu) ----
