@@ -42,6 +42,13 @@ WORKLOADS = {
     "sdgc-16384x1920": (16384, 1920, 60000, -0.40, 30),
     "sdgc-65536x1920": (65536, 1920, 60000, -0.45, 30),
 }
+# RadiX-Net-structured nets (radix 2, dense blocks of 16, weights 1/16): extra
+# lines only (--extra-workloads)
+RADIXNET = {
+    "radixnet-1024x120": (1024, 120, 60000, -0.30, 30),
+    "radixnet-4096x480": (4096, 480, 60000, -0.35, 30),
+    "radixnet-65536x1920": (65536, 1920, 60000, -0.45, 30),
+}
 SEED = 20260101
 NNZ = 32
 METRIC = "edges/s & ms/inference, SNICIT vs plain on 1 GB300 (exact categories); p50/p99"
@@ -607,7 +614,7 @@ def run_extra(args, sg, torch, workload, local):
     """Another SDGC workload on the same GPU, reported as an extra key: SNICIT
     (autotuned) and the plain path, device-resident inputs."""
     import numpy as np
-    N, L, B, bias, t_default = WORKLOADS[workload]
+    N, L, B, bias, t_default = WORKLOADS[workload] if workload in WORKLOADS else RADIXNET[workload]
     dev = f"cuda:{local}"
     d_in = torch.empty((B, N), dtype=torch.float32, device=dev)
     sg.generate_inputs_device(N, SEED, 0, B, d_in.data_ptr())
@@ -615,7 +622,10 @@ def run_extra(args, sg, torch, workload, local):
     stream = torch.cuda.current_stream()
     with sg.Engine(N, L, mode="SNICIT", threshold=t_default, batch=B, bias=bias,
                    num_centroids=args.centroids, device=local) as eng:
-        eng.generate_weights(SEED, NNZ, 0.0625)
+        if workload in RADIXNET:
+            eng.generate_radixnet(16, 0.0625)
+        else:
+            eng.generate_weights(SEED, NNZ, 0.0625)
         eng.finalize()
         autotune(eng, args, workload, d_in.data_ptr(), B)
         fn = lambda: eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr(), stream.cuda_stream)
@@ -880,7 +890,7 @@ def main():
                     help="live rows and activation density per layer of --workload")
     ap.add_argument("--density-rows", type=int, default=8192)
     ap.add_argument("--density-layers", type=int, default=12)
-    ap.add_argument("--extra-workloads", default="sdgc-4096x480",
+    ap.add_argument("--extra-workloads", default="sdgc-4096x480,radixnet-4096x480",
                     help="comma-separated workloads reported as extra keys")
     ap.add_argument("--e2e-steps", type=int, default=5,
                     help="host-API calls timed per end-to-end form (median)")

@@ -192,6 +192,20 @@ int sdnn_set_layer_bias(sdnn_engine* e, int32_t layer, const float* bias);
  * (seed, layer, row). */
 int sdnn_generate_weights(sdnn_engine* e, uint64_t seed, int32_t nnz_per_row, float value);
 
+/* RadiX-Net-structured weights (Robinett and Kepner, "RadiX-Net: Structured
+ * Sparse Matrices for Deep Neural Networks", 2019): a radix-2 topology on
+ * M = N / block nodes (M a power of two, M >= 2) Kronecker-multiplied with
+ * dense blocks of `block` neurons.  Neuron v is (dense index v / M, node
+ * v % M); in layer l every output of node c reads every input of nodes c and
+ * c + 2^(l mod log2 M) (mod M), all with `value`: 2 * block in-edges per
+ * output and out-edges per input.  block = 16 with value 1/16 is the layout
+ * the reference's SNICIT / XY kernels are written for: its HashReorder
+ * (src/SDGC/reorder/hash.h:14-22, buckets = M) makes every node's 16 neurons
+ * contiguous, and its layers 0 .. log2 M - 1 read node c + 16 * 2^l / 16
+ * (src/SDGC/SNICIT/SNICIT.hpp:329-342, src/SDGC/XY/kernel.hpp:12-101).
+ * SDNN_ERR_INVALID for other shapes. */
+int sdnn_generate_radixnet_weights(sdnn_engine* e, int32_t block, float value);
+
 /* Packs the host weights into the device layout (bank-scheduled slots) and
  * uploads them.  Called implicitly by the first inference. */
 int sdnn_finalize_weights(sdnn_engine* e);
@@ -406,6 +420,11 @@ int sdnn_generate_inputs_device(int32_t num_neurons, uint64_t seed, int64_t row_
 int sdnn_generate_layer_coo(int32_t num_neurons, uint64_t seed, int32_t layer,
                             int32_t nnz_per_row, float value, int32_t* rows,
                             int32_t* cols, float* vals);
+
+/* One RadiX-Net layer (sdnn_generate_radixnet_weights) as COO, input-major,
+ * each input's outputs ascending (rows/cols/vals each num_neurons * 2 * block). */
+int sdnn_generate_radixnet_layer_coo(int32_t num_neurons, int32_t block, int32_t layer,
+                                     float value, int32_t* rows, int32_t* cols, float* vals);
 
 /* Binary input files (no reference counterpart; they replace parsing the
  * input TSV, src/SDGC/utility.hpp:160-191): encoding 0 = FP32 rows, 1 = one

@@ -42,6 +42,9 @@ def lib():
         L.oracle_gen_layer_csr.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_float, P, P, P]
         L.oracle_gen_layer_csr.restype = ctypes.c_int
+        L.oracle_gen_radixnet_csr.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_float, P, P, P]
+        L.oracle_gen_radixnet_csr.restype = ctypes.c_int
         L.oracle_port_stream.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
                                          ctypes.c_float, ctypes.c_float, ctypes.c_float, P,
                                          ctypes.c_int64, P, ctypes.c_int, ctypes.c_int, P, P]
@@ -164,6 +167,18 @@ def gen_layer_csr(N, seed, layer, nnz=32, value=0.0625):
     if lib().oracle_gen_layer_csr(int(N), int(seed), int(layer), int(nnz), float(value), _p(ro),
                                   _p(cols), _p(vals)):
         raise RuntimeError("oracle_gen_layer_csr failed")
+    return ro, cols, vals
+
+
+def gen_radixnet_csr(N, layer, block=16, value=0.0625):
+    """One RadiX-Net layer (radix 2, dense blocks of `block`) as CSR by input
+    row, stated output by output (restated generator)."""
+    ro = np.zeros(N + 1, dtype=np.int32)
+    cols = np.zeros(N * 2 * block, dtype=np.int32)
+    vals = np.zeros(N * 2 * block, dtype=np.float32)
+    if lib().oracle_gen_radixnet_csr(int(N), int(block), int(layer), float(value), _p(ro),
+                                     _p(cols), _p(vals)):
+        raise RuntimeError("oracle_gen_radixnet_csr failed")
     return ro, cols, vals
 
 

@@ -495,6 +495,44 @@ int oracle_gen_layer_csr(int N, uint64_t seed, int layer, int nnz, float value, 
   return 0;
 }
 
+/* RadiX-Net layer, radix 2 with dense blocks of `block` neurons (Robinett and
+ * Kepner, 2019): N = block * M, M = 2^k nodes, neuron v = (v / M, node v % M).
+ * Stated output by output -- output (r, c) reads every input of nodes c and
+ * c + 2^(layer mod k) (mod M), the windows the reference's XY kernels read
+ * after its HashReorder (src/SDGC/XY/kernel.hpp:71-91, strides from
+ * src/SDGC/SNICIT/SNICIT.hpp:329-342) -- then turned into CSR by input row
+ * (outputs ascending). */
+int oracle_gen_radixnet_csr(int N, int block, int layer, float value, int32_t* row_off,
+                            int32_t* cols, float* vals) {
+  if (block < 1 || N < 2 * block || N % block != 0 || layer < 0) return 1;
+  const int M = N / block;
+  if (M & (M - 1)) return 1;
+  int k = 0;
+  while ((1 << k) < M) ++k;
+  const int step = 1 << (layer % k);
+  for (int i = 0; i <= N; ++i) row_off[i] = 0;
+  for (int out = 0; out < N; ++out) {
+    const int nodes[2] = {out % M, (out % M + step) % M};
+    for (int n = 0; n < 2; ++n)
+      for (int r = 0; r < block; ++r) row_off[r * M + nodes[n] + 1]++;
+  }
+  for (int i = 0; i < N; ++i) row_off[i + 1] += row_off[i];
+  int32_t* cur = (int32_t*)malloc(sizeof(int32_t) * (size_t)N);
+  if (!cur) return 1;
+  for (int i = 0; i < N; ++i) cur[i] = row_off[i];
+  for (int out = 0; out < N; ++out) {
+    const int nodes[2] = {out % M, (out % M + step) % M};
+    for (int n = 0; n < 2; ++n)
+      for (int r = 0; r < block; ++r) {
+        const int in = r * M + nodes[n];
+        cols[cur[in]] = out;
+        vals[cur[in]++] = value;
+      }
+  }
+  free(cur);
+  return 0;
+}
+
 /* ---- FP32 port over groups of rows, weights generated layer by layer ---- */
 
 static double now_s(void) {

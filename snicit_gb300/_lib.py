@@ -95,6 +95,7 @@ SIGNATURES = [
     ("sdnn_set_layer_coo", ctypes.c_int, [P, I32, P, P, P, I64]),
     ("sdnn_set_layer_bias", ctypes.c_int, [P, I32, P]),
     ("sdnn_generate_weights", ctypes.c_int, [P, U64, I32, F32]),
+    ("sdnn_generate_radixnet_weights", ctypes.c_int, [P, I32, F32]),
     ("sdnn_finalize_weights", ctypes.c_int, [P]),
     ("sdnn_infer_host", ctypes.c_int, [P, P, I64, P, P, P]),
     ("sdnn_infer_device", ctypes.c_int, [P, P, I64, P, P]),
@@ -125,6 +126,7 @@ SIGNATURES = [
     ("sdnn_generate_inputs", ctypes.c_int, [I32, U64, I64, I64, P]),
     ("sdnn_generate_inputs_device", ctypes.c_int, [I32, U64, I64, I64, P, P]),
     ("sdnn_generate_layer_coo", ctypes.c_int, [I32, U64, I32, I32, F32, P, P, P]),
+    ("sdnn_generate_radixnet_layer_coo", ctypes.c_int, [I32, I32, I32, F32, P, P, P]),
     ("sdnn_write_weights_tsv", ctypes.c_int, [P, ctypes.c_char_p]),
     ("sdnn_write_inputs_tsv", ctypes.c_int, [ctypes.c_char_p, P, I64, I32]),
     ("sdnn_write_categories_tsv", ctypes.c_int, [ctypes.c_char_p, P, I64]),

@@ -27,6 +27,8 @@ namespace sdnn {
 int read_weight_tsv(const std::string& path, int32_t N, HostLayer& out, std::string& err);
 int write_weight_tsv(const std::string& path, const HostLayer& h, int32_t N);
 void gen_row_cols(uint64_t seed, int32_t layer, int32_t row, int32_t N, int32_t nnz, int32_t* cols);
+bool radixnet_shape_ok(int32_t N, int32_t block);
+void radixnet_row_cols(int32_t N, int32_t block, int32_t layer, int32_t row, int32_t* cols);
 }  // namespace sdnn
 
 using namespace sdnn;
@@ -94,6 +96,7 @@ struct GenSpec {
   uint64_t seed = 0;
   int32_t nnz = 32;
   float value = 0.0625f;
+  int32_t radix_block = 0;  // > 0: RadiX-Net layers with dense blocks of this width
 };
 
 }  // namespace
@@ -535,15 +538,19 @@ int ensure_buffers(sdnn_engine* e, int64_t rows) {
 // The host CSR of layer l: regenerated for synthetic weights, else stored.
 const HostLayer* host_layer(sdnn_engine* e, int l, HostLayer& tmp) {
   if (!e->gen.on) return e->hw[l].present ? &e->hw[l] : nullptr;
-  const int N = e->N, k = e->gen.nnz;
+  const int N = e->N, k = e->gen.radix_block > 0 ? 2 * e->gen.radix_block : e->gen.nnz;
   tmp.row_off.resize(N + 1);
   tmp.cols.resize((size_t)N * k);
   tmp.vals.assign((size_t)N * k, e->gen.value);
   for (int j = 0; j < N; ++j) {
     tmp.row_off[j] = j * k;
     int32_t* c = tmp.cols.data() + (size_t)j * k;
-    gen_row_cols(e->gen.seed, l, j, N, k, c);
-    std::sort(c, c + k);
+    if (e->gen.radix_block > 0) {
+      radixnet_row_cols(N, e->gen.radix_block, l, j, c);
+    } else {
+      gen_row_cols(e->gen.seed, l, j, N, k, c);
+      std::sort(c, c + k);
+    }
   }
   tmp.row_off[N] = N * k;
   tmp.present = true;
@@ -1803,6 +1810,25 @@ int sdnn_generate_weights(sdnn_engine* e, uint64_t seed, int32_t nnz_per_row, fl
   e->gen.seed = seed;
   e->gen.nnz = nnz_per_row;
   e->gen.value = value;
+  e->gen.radix_block = 0;
+  for (auto& h : e->hw) h = HostLayer{};
+  e->weights_dirty = true;
+  return SDNN_OK;
+}
+
+int sdnn_generate_radixnet_weights(sdnn_engine* e, int32_t block, float value) {
+  if (!e) return SDNN_ERR_INVALID;
+  if (e->share_users.load() > 0)
+    return fail(e, SDNN_ERR_STATE, "the weights are in use by a server (destroy it first)");
+  if (!radixnet_shape_ok(e->N, block))
+    return fail(e, SDNN_ERR_INVALID,
+                "RadiX-Net needs N = block * M with M a power of two, M >= 2");
+  e->packed.reset();
+  e->gen.on = true;
+  e->gen.seed = 0;
+  e->gen.nnz = 2 * block;
+  e->gen.value = value;
+  e->gen.radix_block = block;
   for (auto& h : e->hw) h = HostLayer{};
   e->weights_dirty = true;
   return SDNN_OK;

@@ -67,7 +67,54 @@ void gen_input_row(uint64_t seed, int64_t row, int32_t N, float* out) {
   for (int32_t j = 0; j < N; ++j) out[j] = unit53(draw(key, 9 + (uint64_t)j)) < rho ? 1.f : 0.f;
 }
 
+// RadiX-Net topology (Robinett and Kepner, "RadiX-Net: Structured Sparse
+// Matrices for Deep Neural Networks", IPDPS workshops 2019): a mixed-radix
+// topology on M nodes, Kronecker-multiplied with dense blocks of width B, so
+// N = B * M.  Here every radix is 2 (M = 2^k) and the k radix layers repeat:
+// in layer l, every output of node c reads every input of nodes c and
+// c + 2^(l mod k) (mod M).  Neuron v is (dense index v / M, node v % M).
+bool radixnet_shape_ok(int32_t N, int32_t block) {
+  if (block < 1 || N < 2 * block || N % block != 0) return false;
+  const int32_t M = N / block;
+  return (M & (M - 1)) == 0;
+}
+
+// Outputs fed by input `row` of RadiX-Net layer `layer`: 2 * block columns,
+// ascending.
+void radixnet_row_cols(int32_t N, int32_t block, int32_t layer, int32_t row, int32_t* cols) {
+  const int32_t M = N / block;
+  int32_t k = 0;
+  while ((1 << k) < M) ++k;
+  const int32_t step = 1 << (layer % k);
+  const int32_t c = row % M;
+  // output nodes whose inputs include node c: c itself and c - step
+  int32_t lo = c, hi = (c - step + M) % M;
+  if (lo > hi) std::swap(lo, hi);
+  int n = 0;
+  for (int32_t r = 0; r < block; ++r) {
+    cols[n++] = r * M + lo;
+    cols[n++] = r * M + hi;
+  }
+}
+
 }  // namespace sdnn
+
+extern "C" int sdnn_generate_radixnet_layer_coo(int32_t num_neurons, int32_t block, int32_t layer,
+                                                float value, int32_t* rows, int32_t* cols,
+                                                float* vals) {
+  if (!sdnn::radixnet_shape_ok(num_neurons, block) || layer < 0 || !rows || !cols || !vals)
+    return SDNN_ERR_INVALID;
+  const int32_t k = 2 * block;
+  for (int32_t j = 0; j < num_neurons; ++j) {
+    const int64_t o = (int64_t)j * k;
+    sdnn::radixnet_row_cols(num_neurons, block, layer, j, cols + o);
+    for (int32_t i = 0; i < k; ++i) {
+      rows[o + i] = j;
+      vals[o + i] = value;
+    }
+  }
+  return SDNN_OK;
+}
 
 extern "C" int sdnn_generate_inputs(int32_t num_neurons, uint64_t seed, int64_t row_offset,
                                     int64_t rows, float* out) {

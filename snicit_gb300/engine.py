@@ -104,6 +104,11 @@ class Engine:
     def generate_weights(self, seed, nnz_per_row=32, value=0.0625):
         self._ck(load().sdnn_generate_weights(self._h, int(seed), int(nnz_per_row), float(value)))
 
+    def generate_radixnet(self, block=16, value=0.0625):
+        """RadiX-Net-structured layers (radix 2, dense blocks of `block`
+        neurons); see sdnn_generate_radixnet_weights."""
+        self._ck(load().sdnn_generate_radixnet_weights(self._h, int(block), float(value)))
+
     def finalize(self):
         self._ck(load().sdnn_finalize_weights(self._h))
 
@@ -244,6 +249,16 @@ def generate_layer_coo(num_neurons, seed, layer, nnz_per_row=32, value=0.0625):
     v = np.zeros(n, dtype=np.float32)
     check(load().sdnn_generate_layer_coo(int(num_neurons), int(seed), int(layer), int(nnz_per_row),
                                          float(value), _ptr(r), _ptr(c), _ptr(v)))
+    return r, c, v
+
+
+def generate_radixnet_layer_coo(num_neurons, layer, block=16, value=0.0625):
+    n = num_neurons * 2 * block
+    r = np.zeros(n, dtype=np.int32)
+    c = np.zeros(n, dtype=np.int32)
+    v = np.zeros(n, dtype=np.float32)
+    check(load().sdnn_generate_radixnet_layer_coo(int(num_neurons), int(block), int(layer),
+                                                  float(value), _ptr(r), _ptr(c), _ptr(v)))
     return r, c, v
 
 

@@ -128,3 +128,58 @@ def test_streamed_fp64_oracle_equals_the_fp64_oracle():
     Y, alive = orc.infer_stream64(N, L, seed, bias, Y0, nthreads=3)
     assert np.array_equal(alive, alive_w) and 0 < alive.sum() < 200
     assert np.array_equal(Y, want)
+
+
+# ---- RadiX-Net-structured layers --------------------------------------------
+
+def _hash(v, M, width=16):
+    """The reference's HashReorder (src/SDGC/reorder/hash.h:14-22) with M
+    buckets of `width`: v -> v / M + (v % M) * width."""
+    return v // M + (v % M) * width
+
+
+def test_radixnet_matches_the_oracle_restatement():
+    from oracle import oracle as orc
+    for N, block in ((1024, 16), (4096, 16), (256, 8), (64, 32)):
+        M = N // block
+        for layer in range(0, 2 * int(np.log2(M)) + 1):
+            r, c, v = sg.generate_radixnet_layer_coo(N, layer, block)
+            ro, oc, ov = orc.gen_radixnet_csr(N, layer, block)
+            assert np.array_equal(np.repeat(np.arange(N), np.diff(ro)), r)
+            assert np.array_equal(oc, c) and np.array_equal(ov, v)
+
+
+def test_radixnet_structure_is_the_one_the_reference_kernels_read():
+    """Every output has 32 in-edges and every input 32 out-edges; after the
+    reference's hash reorder, output node c (16 consecutive outputs) reads the
+    16 inputs of node c and the 16 of node c + stride / 16, with the
+    reference's strides 16 * 2^l for layers 0 .. log2(M) - 1
+    (src/SDGC/SNICIT/SNICIT.hpp:329-342, src/SDGC/XY/kernel.hpp:24-35,71-91),
+    and the same cycle again after that."""
+    for N in (1024, 4096, 16384):
+        M = N // 16
+        k = int(np.log2(M))
+        for layer in list(range(k + 2)) + [119]:
+            r, c, _ = sg.generate_radixnet_layer_coo(N, layer, 16)
+            assert np.array_equal(np.bincount(r, minlength=N), np.full(N, 32))
+            assert np.array_equal(np.bincount(c, minlength=N), np.full(N, 32))
+            hr, hc = _hash(r, M), _hash(c, M)
+            stride = 16 * 2 ** (layer % k)
+            for node in (0, 1, M // 2, M - 1):
+                ins = np.unique(hr[hc // 16 == node])
+                want = np.concatenate([node * 16 + np.arange(16),
+                                       (node * 16 + stride + np.arange(16)) % N])
+                assert np.array_equal(ins, np.sort(want)), (N, layer, node)
+
+
+def test_radixnet_rejects_shapes_without_a_power_of_two_node_count():
+    import ctypes
+    n = 48 * 32
+    r = np.zeros(n, np.int32)
+    c = np.zeros(n, np.int32)
+    v = np.zeros(n, np.float32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    L = sg.load()
+    assert L.sdnn_generate_radixnet_layer_coo(48 * 16, 16, 0, 0.0625, P(r), P(c), P(v)) != 0
+    assert L.sdnn_generate_radixnet_layer_coo(1024, 0, 0, 0.0625, P(r), P(c), P(v)) != 0
+    assert L.sdnn_generate_radixnet_layer_coo(16, 16, 0, 0.0625, P(r), P(c), P(v)) != 0

@@ -51,10 +51,11 @@ def _run_device(torch, eng, d_in, B):
     return d_flags.cpu().numpy().copy()
 
 
-def _ref_harness(tmp_path, N, L, bias, Y0):
+def _ref_harness(tmp_path, N, L, bias, Y0, layers=None):
     """Runs the reference's bf_inference / snig_inference (built from its
-    sources into oracle/_ref/) on the synthetic net; returns (Y_bf, Y_snig)
-    or None when the reference kernels are not built here."""
+    sources into oracle/_ref/) on the synthetic net (or on `layers`, CSR by
+    input row); returns (Y_bf, Y_snig) or None when the reference kernels are
+    not built here."""
     module = os.path.join(ROOT, "oracle", "_ref", "sdgc_ref.cubin")
     if not os.path.exists(module):
         return None
@@ -66,7 +67,7 @@ def _ref_harness(tmp_path, N, L, bias, Y0):
     with open(inp, "wb") as f:
         f.write(struct.pack("<iiiif", N, L, B, N, bias))  # one section: N fits 48 KB of shared memory
         for l in range(L):
-            ro, c, v = orc.gen_layer_csr(N, SEED, l)
+            ro, c, v = layers[l] if layers is not None else orc.gen_layer_csr(N, SEED, l)
             order = np.argsort(c.reshape(N, 32), axis=1, kind="stable")
             c = np.take_along_axis(c.reshape(N, 32), order, 1).ravel()
             f.write(struct.pack("<i", len(c)))
