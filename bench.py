@@ -804,14 +804,21 @@ def run_serving(args, sg, local=0):
     tuned = engines["SNICIT"].autotune(pool[:4096], rec)
     out["snicit_settings"] = {k: tuned[k] for k in ("threshold", "centroid_candidates",
                                                       "merge_start", "tile_rows", "threads")}
-    arms = [("continuous_snicit", "SNICIT", dict(slots=2), arrivals),
-            ("continuous_plain", "SNIG", dict(slots=2), arrivals),
-            ("per_request_plain", "SNIG", dict(slots=1, max_requests_per_pass=1), arrivals),
-            ("saturation_snicit", "SNICIT", dict(slots=2), np.zeros_like(arrivals)),
-            ("saturation_plain", "SNIG", dict(slots=2), np.zeros_like(arrivals))]
+    # continuous batching: four slots of at most 4096 rows each, so a request
+    # that arrives during a pass waits for a short pass, not a 16384-row one;
+    # saturation: two slots of 16384 rows (throughput)
+    live = dict(slots=4, max_rows=4096)
+    bulk = dict(slots=2, max_rows=16384)
+    arms = [("continuous_snicit", "SNICIT", live, arrivals),
+            ("continuous_plain", "SNIG", live, arrivals),
+            ("per_request_plain", "SNIG", dict(slots=1, max_requests_per_pass=1, max_rows=16384),
+             arrivals),
+            ("saturation_snicit", "SNICIT", bulk, np.zeros_like(arrivals)),
+            ("saturation_plain", "SNIG", bulk, np.zeros_like(arrivals))]
+    out["continuous_server"] = live
     for name, mode, kw, arr in arms:
         lat, rows, wall, st = serve_stream(sg, engines[mode], hw, hb, pool, arr, sizes, offsets,
-                                           max_rows=16384, **kw)
+                                           **kw)
         out[name] = {"samples_per_s": rows / wall, "p50_ms": _percentile(lat, 0.5) * 1e3,
                      "p99_ms": _percentile(lat, 0.99) * 1e3, "passes": st["passes"],
                      "max_rows_in_pass": st["max_rows_in_pass"], "wall_s": wall}
