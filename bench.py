@@ -769,14 +769,9 @@ def serve_stream(sg, eng, head_w, head_b, pool, arrivals, sizes, offsets, **serv
     return lat, int(sum(sizes)), wall, st
 
 
-def run_serving(args, sg, local=0):
-    """Serving loop on the sparse MLP (1024 inputs, 120 layers of width 1024 at
-    3% density, N(0, 0.3^2) weights, bias -0.05, clamp 32, dense 1024x10 head):
-    a seeded Poisson stream of requests (sizes log-uniform in [1, 4096]) at
-    --serve-rate req/s, replayed in real time against the continuous-batching
-    server (SNICIT mode, clustering across co-resident requests, and SNIG
-    mode), against the per-request path (one request per pass, SNIG), and at
-    saturation (all requests queued at once)."""
+def serving_setup(args, sg, local=0):
+    """The serving workload: the sparse MLP, the request stream, the input
+    pool and one engine per mode (the SNICIT one autotuned)."""
     import numpy as np
     N, L = 1024, 120
     layers, hw, hb = sg.sparse_mlp(SEED, N=N, L=L)
@@ -784,9 +779,6 @@ def run_serving(args, sg, local=0):
     pool = sg.mlp_inputs(SEED, 0, 16384, N)
     rng = np.random.default_rng([SEED, 5])
     offsets = [int(rng.integers(0, len(pool) - n + 1)) for n in sizes]
-    out = {"workload": f"serve-mlp-{N}x{L}", "requests": len(sizes), "rate_req_s": args.serve_rate,
-           "rows": int(sizes.sum()), "mean_rows": float(sizes.mean()),
-           "arrival_span_s": float(arrivals[-1])}
     engines = {}
     for mode in ("SNICIT", "SNIG"):
         e = sg.Engine(N, L, mode=mode, threshold=30, batch=4096, bias=-0.05, num_centroids=50,
@@ -802,6 +794,45 @@ def run_serving(args, sg, local=0):
     if os.path.exists(rec):
         os.remove(rec)
     tuned = engines["SNICIT"].autotune(pool[:4096], rec)
+    return dict(N=N, L=L, hw=hw, hb=hb, arrivals=arrivals, sizes=sizes, pool=pool,
+                offsets=offsets, engines=engines, tuned=tuned)
+
+
+def run_serve_sweep(args, sg):
+    """Slots x rows-per-slot grid of the continuous-batching server on the
+    serving workload; one JSON line per point."""
+    w = serving_setup(args, sg)
+    for mode in ("SNIG", "SNICIT"):
+        for slots in (1, 2, 3, 4, 6):
+            for max_rows in (16384, 8192, 4096):
+                lat, rows, wall, st = serve_stream(sg, w["engines"][mode], w["hw"], w["hb"],
+                                                   w["pool"], w["arrivals"], w["sizes"],
+                                                   w["offsets"], slots=slots, max_rows=max_rows)
+                print(json.dumps({"mode": mode, "slots": slots, "max_rows": max_rows,
+                                  "p50_ms": _percentile(lat, 0.5) * 1e3,
+                                  "p99_ms": _percentile(lat, 0.99) * 1e3,
+                                  "samples_per_s": rows / wall, "passes": st["passes"]}),
+                      flush=True)
+    for e in w["engines"].values():
+        e.close()
+
+
+def run_serving(args, sg, local=0):
+    """Serving loop on the sparse MLP (1024 inputs, 120 layers of width 1024 at
+    3% density, N(0, 0.3^2) weights, bias -0.05, clamp 32, dense 1024x10 head):
+    a seeded Poisson stream of requests (sizes log-uniform in [1, 4096]) at
+    --serve-rate req/s, replayed in real time against the continuous-batching
+    server (SNICIT mode, clustering across co-resident requests, and SNIG
+    mode), against the per-request path (one request per pass, SNIG), and at
+    saturation (all requests queued at once)."""
+    import numpy as np
+    w = serving_setup(args, sg, local)
+    N, L, hw, hb, pool = w["N"], w["L"], w["hw"], w["hb"], w["pool"]
+    arrivals, sizes, offsets, engines, tuned = (w["arrivals"], w["sizes"], w["offsets"],
+                                                w["engines"], w["tuned"])
+    out = {"workload": f"serve-mlp-{N}x{L}", "requests": len(sizes), "rate_req_s": args.serve_rate,
+           "rows": int(sizes.sum()), "mean_rows": float(sizes.mean()),
+           "arrival_span_s": float(arrivals[-1])}
     out["snicit_settings"] = {k: tuned[k] for k in ("threshold", "centroid_candidates",
                                                       "merge_start", "tile_rows", "threads")}
     # continuous batching: four slots of at most 4096 rows each, so a request
@@ -906,6 +937,8 @@ def main():
     ap.add_argument("--serve-only", action="store_true", help="only the serving-loop measurement")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-sweep", action="store_true",
+                    help="slots x rows-per-slot grid of the serving loop, one JSON line each")
     ap.add_argument("--case", default=None, choices=sorted(CASES),
                     help="run a small fixed case (used for ncu captures) instead of the bench")
     args = ap.parse_args()
@@ -917,6 +950,9 @@ def main():
         import torch
         import snicit_gb300 as sg
         print(json.dumps({"residue_stage": run_residue(args, sg, torch, 0)}), flush=True)
+    elif args.serve_sweep:
+        import snicit_gb300 as sg
+        run_serve_sweep(args, sg)
     elif args.serve_only:
         import snicit_gb300 as sg
         print(json.dumps({"serving": run_serving(args, sg)}), flush=True)
