@@ -173,6 +173,21 @@ int tune(sdnn_engine* e, const Sample& smp, const char* record_path) {
         }
       }
       sdnn::engine_set_merge(e, bm.merge_start, best_every, true);
+      // with merging on, clustering earlier than the sweep's thresholds can
+      // pay (the merged rows may be down to a few centroids sooner): thresholds
+      // below the chosen one and above the first merge, with that merge setting
+      if (bs.threshold < cfg0.num_layers) {
+        Trial bt = bm;
+        for (int th : {12, 16, 20, 24}) {
+          if (th >= bm.threshold || th <= bm.merge_start) continue;
+          sdnn::engine_set_snicit(e, th, bm.centroids);
+          Trial t{bm.tile, bm.threads, th, bm.centroids, bm.merge_start, 0.f, 0, 0};
+          t.status = time_setting(e, smp, -1, t.ms, t.survivors);
+          record(f, "snicit_merged", t, smp.rows);
+          if (t.status == SDNN_OK && t.ms < bt.ms) bt = t;
+        }
+        sdnn::engine_set_snicit(e, bt.threshold, bt.centroids);
+      }
     }
   }
   if (f) std::fclose(f);

@@ -437,7 +437,12 @@ def test_set_mode_and_device_autotune():
     with sg.Engine(N, L, mode="SNICIT", threshold=30, batch=B, bias=-0.3) as eng:
         eng.generate_weights(seed)
         eng.autotune_device(d.data_ptr(), B)
-        assert eng.stats()["threshold"] in (30, 60)
+        # the sweep's thresholds, no clustering (L), or the earlier ones tried with merging
+        assert eng.stats()["threshold"] in (12, 16, 20, 24, 30, 60, L)
+        f.zero_()
+        eng.infer_device(d.data_ptr(), B, f.data_ptr())
+        torch.cuda.synchronize()
+        assert np.array_equal(f.cpu().numpy(), alive), "autotuned"
         for mode, t in (("SNICIT", 30), ("SNIG", L), ("BF", L), ("SNICIT", 60)):
             eng.set_mode(mode, t)
             f.zero_()
