@@ -183,3 +183,19 @@ def test_radixnet_rejects_shapes_without_a_power_of_two_node_count():
     assert L.sdnn_generate_radixnet_layer_coo(48 * 16, 16, 0, 0.0625, P(r), P(c), P(v)) != 0
     assert L.sdnn_generate_radixnet_layer_coo(1024, 0, 0, 0.0625, P(r), P(c), P(v)) != 0
     assert L.sdnn_generate_radixnet_layer_coo(16, 16, 0, 0.0625, P(r), P(c), P(v)) != 0
+
+
+def test_radixnet_weights_are_emitted_as_sdgc_tsv(tmp_path):
+    """An engine with RadiX-Net layers writes them in the SDGC layout
+    (dir/n{N}-l{l}.tsv, 1-based "row col value" lines), the same edges as the
+    generator's COO."""
+    N, L = 256, 5
+    with sg.Engine(N, L, mode="SNIG", batch=4) as eng:
+        eng.generate_radixnet(16, 0.0625)
+        eng.write_weights_tsv(tmp_path)
+    for l in range(L):
+        t = np.loadtxt(tmp_path / f"n{N}-l{l + 1}.tsv", ndmin=2)
+        r, c, v = sg.generate_radixnet_layer_coo(N, l, 16)
+        assert np.array_equal(t[:, 0].astype(np.int64) - 1, r)
+        assert np.array_equal(t[:, 1].astype(np.int64) - 1, c)
+        assert np.allclose(t[:, 2], v)
