@@ -11,6 +11,8 @@ for.  On those nets:
   same category set on the same net.
 * 4096 x 480 x 60000: SNICIT with row merging equals the plain path's
   category set; a seeded 1000-row subset matches the FP64 oracle.
+* 65536 x 120 x 8192 (input chunks): SNICIT == plain; 16 seeded rows (8
+  survivors, 8 not) against the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -86,4 +88,41 @@ def test_radixnet_4096x480_snicit_equals_plain_and_fp64_subset():
     err = _rel_rows(Y[rows], Yref)
     print(f"RadiX-Net 4096x480: {snicit.sum()} survivors, SNICIT == plain; 1000 rows vs FP64 "
           f"max error {err.max():.3g}")
+    assert err.max() <= RTOL
+
+
+def test_radixnet_65536_input_chunks_snicit_equals_plain_and_fp64_rows():
+    """The input-chunked kernels (chunks of 16384) on a RadiX-Net net, whose
+    nodes' 16 outputs all read the same 32 inputs."""
+    torch = pytest.importorskip("torch")
+    N, L, B = 65536, 120, 8192
+    bias = sg.load().sdnn_reference_bias(N)
+    d_in = torch.empty((B, N), dtype=torch.float32, device="cuda")
+    sg.generate_inputs_device(N, SEED, 0, B, d_in.data_ptr())
+    d_flags = torch.zeros(B, dtype=torch.int32, device="cuda")
+    with sg.Engine(N, L, mode="SNICIT", threshold=30, batch=B, bias=bias,
+                   num_centroids=50) as eng:
+        eng.generate_radixnet(16, 0.0625)
+        eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr())
+        torch.cuda.synchronize()
+        snicit = d_flags.cpu().numpy().copy()
+        Y = eng.activations(B)
+        eng.set_mode("SNIG", L)
+        d_flags.zero_()
+        eng.infer_device(d_in.data_ptr(), B, d_flags.data_ptr())
+        torch.cuda.synchronize()
+        plain = d_flags.cpu().numpy().copy()
+    assert np.array_equal(snicit, plain)
+    assert 0 < snicit.sum() < B
+    rng = np.random.default_rng([SEED, 16])
+    live, dead = np.flatnonzero(snicit), np.flatnonzero(snicit == 0)
+    rows = np.sort(np.concatenate([rng.choice(live, min(8, len(live)), replace=False),
+                                   rng.choice(dead, min(8, len(dead)), replace=False)]))
+    Y0s = np.concatenate([orc.gen_inputs(N, SEED, int(r), 1) for r in rows])
+    layers = [orc.gen_radixnet_csr(N, l) for l in range(L)]
+    Yref, alive, _ = orc.infer(layers, N, bias, Y0s, precision=64)
+    assert np.array_equal(snicit[rows], alive)
+    err = _rel_rows(Y[rows], Yref)
+    print(f"RadiX-Net 65536x120: {snicit.sum()} survivors of {B}, SNICIT == plain; "
+          f"{len(rows)} rows vs FP64 max error {err.max():.3g}")
     assert err.max() <= RTOL
