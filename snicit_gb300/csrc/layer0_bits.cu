@@ -32,6 +32,100 @@ __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32
   l = u ^ c;
 }
 
+// Bit-sliced counters c[0..6] (c[i] bit t = bit i of row t's count) plus 16,
+// 8 or 4 words, each word adding 1 to the rows whose bit is set: Harley-Seal
+// carry-save trees, the carry out of the tree rippled into the higher planes.
+__device__ __forceinline__ void ripple(uint32_t (&c)[7], int from, uint32_t cy) {
+#pragma unroll
+  for (int i = 0; i < 7; ++i) {
+    if (i < from) continue;
+    const uint32_t t = c[i] & cy;
+    c[i] ^= cy;
+    cy = t;
+  }
+}
+__device__ __forceinline__ void add16(uint32_t (&c)[7], const uint32_t (&w)[16]) {
+  uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, c16;
+  csa(twosA, c[0], c[0], w[0], w[1]);
+  csa(twosB, c[0], c[0], w[2], w[3]);
+  csa(foursA, c[1], c[1], twosA, twosB);
+  csa(twosA, c[0], c[0], w[4], w[5]);
+  csa(twosB, c[0], c[0], w[6], w[7]);
+  csa(foursB, c[1], c[1], twosA, twosB);
+  csa(eightsA, c[2], c[2], foursA, foursB);
+  csa(twosA, c[0], c[0], w[8], w[9]);
+  csa(twosB, c[0], c[0], w[10], w[11]);
+  csa(foursA, c[1], c[1], twosA, twosB);
+  csa(twosA, c[0], c[0], w[12], w[13]);
+  csa(twosB, c[0], c[0], w[14], w[15]);
+  csa(foursB, c[1], c[1], twosA, twosB);
+  csa(eightsB, c[2], c[2], foursA, foursB);
+  csa(c16, c[3], c[3], eightsA, eightsB);
+  ripple(c, 4, c16);
+}
+__device__ __forceinline__ void add8(uint32_t (&c)[7], const uint32_t* w) {
+  uint32_t twosA, twosB, foursA, foursB, eights;
+  csa(twosA, c[0], c[0], w[0], w[1]);
+  csa(twosB, c[0], c[0], w[2], w[3]);
+  csa(foursA, c[1], c[1], twosA, twosB);
+  csa(twosA, c[0], c[0], w[4], w[5]);
+  csa(twosB, c[0], c[0], w[6], w[7]);
+  csa(foursB, c[1], c[1], twosA, twosB);
+  csa(eights, c[2], c[2], foursA, foursB);
+  ripple(c, 3, eights);
+}
+__device__ __forceinline__ void add4(uint32_t (&c)[7], const uint32_t* w) {
+  uint32_t twosA, twosB, fours;
+  csa(twosA, c[0], c[0], w[0], w[1]);
+  csa(twosB, c[0], c[0], w[2], w[3]);
+  csa(fours, c[1], c[1], twosA, twosB);
+  ripple(c, 2, fours);
+}
+
+// Bit words of the slots of K blocks (block b0 onwards; indices ip, lane-
+// strided) from the shared row `bits` (BYTES: indices are byte offsets).
+template <bool BYTES, int K>
+__device__ __forceinline__ void gather_words(uint32_t* w, const uint2* __restrict__ ip, int b0,
+                                             const uint32_t* bits) {
+  uint2 iv[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) iv[k] = __ldg(ip + (size_t)(b0 + k) * 32);
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const uint32_t j = ((s < 2 ? iv[k].x : iv[k].y) >> ((s & 1) * 16)) & 0xffffu;
+      w[k * 4 + s] = BYTES ? *reinterpret_cast<const uint32_t*>(
+                                 reinterpret_cast<const char*>(bits) + j)
+                           : bits[j];
+    }
+  }
+}
+
+// Adds the slots of a list of nb blocks into the counters: 4 blocks at a
+// time, then 2, then 1 (no adder work on blocks past the list's end).
+template <bool BYTES>
+__device__ __forceinline__ void count_list(uint32_t (&c)[7], const uint2* __restrict__ ip, int nb,
+                                           const uint32_t* bits) {
+  int b = 0;
+  for (; b + 4 <= nb; b += 4) {
+    uint32_t w[16];
+    gather_words<BYTES, 4>(w, ip, b, bits);
+    add16(c, w);
+  }
+  if (b + 2 <= nb) {
+    uint32_t w[8];
+    gather_words<BYTES, 2>(w, ip, b, bits);
+    add8(c, w);
+    b += 2;
+  }
+  if (b < nb) {
+    uint32_t w[4];
+    gather_words<BYTES, 1>(w, ip, b, bits);
+    add4(c, w);
+  }
+}
+
 // ---- epilogue: per-row counts out of the bit-sliced counters ----------------
 //
 // Rows of a tile are bits of the counter planes P[0..6] (P[i] bit t = bit i of
@@ -230,48 +324,8 @@ __global__ void __launch_bounds__(256, 3) layer0_bits_kernel(const Layer0Args a)
       const int32_t b0 = __ldg(a.grp_blk + g);
       const int32_t b1 = __ldg(a.grp_blk + g + 1);
       const uint2* __restrict__ ip = a.idx + (size_t)b0 * 32 + lane;
-      uint32_t ones = 0, twos = 0, fours = 0, eights = 0, sixteens = 0, thirtytwos = 0,
-               sixtyfours = 0;
-      for (int b = 0; b < b1 - b0; b += 4) {
-        uint32_t w[16];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          // blocks past the group's end read word 0 (in bounds) and add nothing
-          uint2 iv = make_uint2(0u, 0u);
-          if (b + k < b1 - b0) iv = __ldg(ip + (size_t)(b + k) * 32);
-#pragma unroll
-          for (int s = 0; s < 4; ++s) {
-            const uint32_t word = s < 2 ? iv.x : iv.y;
-            const uint32_t j = (word >> ((s & 1) * 16)) & 0xffffu;
-            const uint32_t* p = rsw_in_bytes(RSW)
-                                    ? reinterpret_cast<const uint32_t*>(
-                                          reinterpret_cast<const char*>(bits) + j)
-                                    : bits + j;
-            w[k * 4 + s] = (b + k < b1 - b0) ? *p : 0u;
-          }
-        }
-        uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, c16;
-        csa(twosA, ones, ones, w[0], w[1]);
-        csa(twosB, ones, ones, w[2], w[3]);
-        csa(foursA, twos, twos, twosA, twosB);
-        csa(twosA, ones, ones, w[4], w[5]);
-        csa(twosB, ones, ones, w[6], w[7]);
-        csa(foursB, twos, twos, twosA, twosB);
-        csa(eightsA, fours, fours, foursA, foursB);
-        csa(twosA, ones, ones, w[8], w[9]);
-        csa(twosB, ones, ones, w[10], w[11]);
-        csa(foursA, twos, twos, twosA, twosB);
-        csa(twosA, ones, ones, w[12], w[13]);
-        csa(twosB, ones, ones, w[14], w[15]);
-        csa(foursB, twos, twos, twosA, twosB);
-        csa(eightsB, fours, fours, foursA, foursB);
-        csa(c16, eights, eights, eightsA, eightsB);
-        uint32_t c = c16, t;
-        t = sixteens & c; sixteens ^= c; c = t;
-        t = thirtytwos & c; thirtytwos ^= c; c = t;
-        sixtyfours ^= c;
-      }
-      const uint32_t P[7] = {ones, twos, fours, eights, sixteens, thirtytwos, sixtyfours};
+      uint32_t P[7] = {0u, 0u, 0u, 0u, 0u, 0u, 0u};
+      count_list<rsw_in_bytes(RSW)>(P, ip, b1 - b0, bits);
       m |= bits_epilogue(P, a, s_sum, s_val, iv, s_rows, nrows, g * 32 + lane, lane);
     }
     if (lane == 0 && m) atomicOr(&s_mask, m);
@@ -355,46 +409,6 @@ __global__ void __launch_bounds__(256) bits_transpose_kernel(const Layer0Args a)
   }
 }
 
-// Adds the slot words of nb blocks (indices ip, lane-strided) into bit-sliced
-// counters; the same carry-save tree as layer0_bits_kernel.
-__device__ __forceinline__ void count_blocks(uint32_t (&c)[7], const uint2* __restrict__ ip, int nb,
-                                             const uint32_t* bits) {
-  for (int b = 0; b < nb; b += 4) {
-    uint32_t w[16];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      uint2 iv = make_uint2(0u, 0u);
-      if (b + k < nb) iv = __ldg(ip + (size_t)(b + k) * 32);
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {
-        const uint32_t word = s < 2 ? iv.x : iv.y;
-        const uint32_t j = (word >> ((s & 1) * 16)) & 0xffffu;
-        w[k * 4 + s] = (b + k < nb) ? bits[j] : 0u;
-      }
-    }
-    uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, c16;
-    csa(twosA, c[0], c[0], w[0], w[1]);
-    csa(twosB, c[0], c[0], w[2], w[3]);
-    csa(foursA, c[1], c[1], twosA, twosB);
-    csa(twosA, c[0], c[0], w[4], w[5]);
-    csa(twosB, c[0], c[0], w[6], w[7]);
-    csa(foursB, c[1], c[1], twosA, twosB);
-    csa(eightsA, c[2], c[2], foursA, foursB);
-    csa(twosA, c[0], c[0], w[8], w[9]);
-    csa(twosB, c[0], c[0], w[10], w[11]);
-    csa(foursA, c[1], c[1], twosA, twosB);
-    csa(twosA, c[0], c[0], w[12], w[13]);
-    csa(twosB, c[0], c[0], w[14], w[15]);
-    csa(foursB, c[1], c[1], twosA, twosB);
-    csa(eightsB, c[2], c[2], foursA, foursB);
-    csa(c16, c[3], c[3], eightsA, eightsB);
-    uint32_t cy = c16, t;
-    t = c[4] & cy; c[4] ^= cy; cy = t;
-    t = c[5] & cy; c[5] ^= cy; cy = t;
-    c[6] ^= cy;
-  }
-}
-
 __global__ void __launch_bounds__(kChunkWarps * 32) bits_count_chunked_kernel(const Layer0Args a) {
   extern __shared__ __align__(128) uint32_t cbits[];  // Q + 32 words
   __shared__ __align__(8) uint64_t bar;
@@ -456,7 +470,7 @@ __global__ void __launch_bounds__(kChunkWarps * 32) bits_count_chunked_kernel(co
         const int g = sub * per_item + k * kChunkWarps + warp;
         if (g < a.G) {
           const int32_t b0 = __ldg(a.grp_blk + g * nq + q), b1 = __ldg(a.grp_blk + g * nq + q + 1);
-          count_blocks(c[k], a.idx + (size_t)b0 * 32 + lane, b1 - b0, cbits);
+          count_list<false>(c[k], a.idx + (size_t)b0 * 32 + lane, b1 - b0, cbits);
         }
       }
     }
