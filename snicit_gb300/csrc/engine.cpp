@@ -163,6 +163,7 @@ struct sdnn_engine {
   float* d_gscratch = nullptr;     // grid chain: [2][8][nq][Q + 32] centroid rows
   unsigned int* d_gbar = nullptr;  // grid chain barrier counter
   uint32_t* d_bits = nullptr;      // chunked binary first layer: bit words per 32-row tile
+  int64_t bits_tile0 = 0;          // first tile of d_bits / d_tile_state the next launch uses
   int32_t* d_tile_state = nullptr;
   // merging of identical rows (SNICIT, below the threshold)
   int32_t* d_alias = nullptr;          // [cap] -1 or the row this row was merged into
@@ -1007,8 +1008,8 @@ int enqueue_layer(sdnn_engine* e, int l, const float* in, const int32_t* lin, co
     // input chunks: transpose pass + counting pass
     b.nq = e->nq;
     b.Q = e->Q;
-    b.bits = e->d_bits;
-    b.tile_state = e->d_tile_state;
+    b.bits = e->d_bits + e->bits_tile0 * e->N;
+    b.tile_state = e->d_tile_state + e->bits_tile0;
     b.tile_mask = e->d_tmask;
     b.tile_ticket = e->d_ticket;
     b.err = e->d_err;
@@ -1064,14 +1065,21 @@ int enqueue_piece(sdnn_engine* e, int p, int64_t r0, int64_t n, int m, const flo
   launch_set_scalar(pc, (int32_t)n, e->stream);
   e->launches++;
   CK(cudaGetLastError());
+  // the piece's bit words (binary layer 0 with input chunks) go to its own
+  // tiles of the buffer (pieces start on 32-row tiles), so both lanes may run
+  e->bits_tile0 = r0 / 32;
   for (int l = 0; l < m; ++l) {
     const float* in = l == 0 ? d_in : e->d_y[(l - 1) & 1];
     const bool last = l + 1 == m;
     int32_t* lout = last ? e->d_list[m & 1] : e->d_plist[(l + 1) & 1] + r0;
     int32_t* cout = last ? e->d_counts + m : pc + l + 1;
     int rc = enqueue_layer(e, l, in, e->d_plist[l & 1] + r0, pc + l, lout, cout);
-    if (rc) return rc;
+    if (rc) {
+      e->bits_tile0 = 0;
+      return rc;
+    }
   }
+  e->bits_tile0 = 0;
   return SDNN_OK;
 }
 
@@ -1941,8 +1949,8 @@ int run_streamed(sdnn_engine* e, const float* Y0, int64_t n, int m, int P) {
   // identity rows into the pieces' layer-0 lists
   launch_begin_rows(e->d_rows, e->d_plist[0], e->d_counts, e->d_flags, e->d_state, e->d_alias, s);
   e->launches += 2;
-  // two lanes (the chunked binary layer 0 has one set of bit buffers: one lane)
-  const bool two = !e->bits_chunked;
+  // two lanes: even and odd pieces
+  const bool two = true;
   if (two) {
     CK(cudaEventRecord(e->lane_ev, s));
     CK(cudaStreamWaitEvent(e->stream2, e->lane_ev, 0));
